@@ -1,0 +1,184 @@
+"""Build the reference's own C for a mechanism (TEST INFRASTRUCTURE).
+
+Recipe, two steps:
+
+``generate``  (needs the reference checkout, default /root/reference)
+    Copies the reference's five Python modules into a scratch directory,
+    applies the minimal Python 3 patch (``except Exception, e`` ->
+    ``as e`` and ``iteritems`` in chem_utilities.py; ``range`` ->
+    ``list(range(...))`` for the species maps in utils.py; ``xrange`` ->
+    ``range`` in create_rate_subs.py), runs the reference's
+    ``create_rate_subs('c', mech, therm)`` in a scratch working directory
+    and copies the emitted ``chem_utils.c``, ``rxn_rates.c``,
+    ``rxn_rates_pres_mod.c``, ``spec_rates.c`` and their headers into
+    ``oracle/_ref/<name>/``.  Nothing is written to the reference checkout.
+
+``compile``  (needs only ``oracle/_ref/<name>/`` and ``oracle/ref_harness.c``)
+    Compiles the emitted files with the batch driver into
+    ``oracle/_ref/<name>/libref.so`` (``-O2 -ffp-contract=off``: the parity
+    build) and ``libref_omp.so`` (``-O3 -fopenmp``: the timed CPU baseline).
+
+``oracle/_ref/`` is git-ignored; the emitted sources travel with the
+working tree so that ``compile`` can run on another host.
+
+Usage: python oracle/build_ref.py {generate,compile,all} NAME [NAME ...]
+       (NAME is a key of create_rate_subs_gb300.synth.CONFIGS)
+"""
+
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+REF_OUT = os.path.join(HERE, "_ref")
+EMITTED = ("chem_utils.c", "rxn_rates.c", "rxn_rates_pres_mod.c",
+           "spec_rates.c", "header.h", "rates.h", "chem_utils.h")
+
+_PATCHES = {
+    "chem_utilities.py": [("except Exception, e:", "except Exception as e:"),
+                          (".iteritems()", ".items()")],
+    "utils.py": [("fwd_species_map = range(num_specs)",
+                  "fwd_species_map = list(range(num_specs))"),
+                 ("back_species_map = range(num_specs)",
+                  "back_species_map = list(range(num_specs))")],
+    "create_rate_subs.py": [("xrange(", "range(")],
+}
+
+
+def ref_dir(name):
+    return os.path.join(REF_OUT, name)
+
+
+def generate(name, mech_path, therm_path, reference="/root/reference",
+             last_spec=None):
+    """Emit the reference's C for one mechanism into oracle/_ref/<name>/."""
+    if not os.path.isdir(reference):
+        raise FileNotFoundError("reference checkout not found: " + reference)
+    mech_path = os.path.abspath(mech_path)
+    therm_path = os.path.abspath(therm_path) if therm_path else None
+    with tempfile.TemporaryDirectory(prefix="crs_refgen_") as tmp:
+        src = os.path.join(tmp, "src")
+        os.makedirs(src)
+        for fn in ("chem_utilities.py", "create_rate_subs.py",
+                   "mech_interpret.py", "rate_subs.py", "utils.py"):
+            with open(os.path.join(reference, fn)) as f:
+                text = f.read()
+            for old, new in _PATCHES.get(fn, []):
+                if old not in text:
+                    raise RuntimeError("patch target %r missing in %s" % (old, fn))
+                text = text.replace(old, new)
+            with open(os.path.join(src, fn), "w") as f:
+                f.write(text)
+        work = os.path.join(tmp, "work")
+        os.makedirs(work)
+        code = ("import sys, warnings\n"
+                "warnings.simplefilter('ignore')\n"
+                "sys.path.insert(0, %r)\n"
+                "import create_rate_subs as crs\n"
+                "crs.create_rate_subs('c', %r, %r, %r)\n"
+                % (src, mech_path, therm_path, last_spec))
+        res = subprocess.run([sys.executable, "-c", code], cwd=work,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference generator failed:\n" + res.stdout
+                               + res.stderr)
+        out = os.path.join(work, "out")
+        dst = ref_dir(name)
+        if os.path.isdir(dst):
+            shutil.rmtree(dst)
+        os.makedirs(dst)
+        for fn in EMITTED:
+            p = os.path.join(out, fn)
+            if os.path.exists(p):
+                shutil.copy(p, dst)
+        with open(os.path.join(dst, "generator.log"), "w") as f:
+            f.write(res.stdout + res.stderr)
+    return dst
+
+
+def _max_index(text, array):
+    idx = [int(m) for m in re.findall(re.escape(array) + r"\[(\d+)\]", text)]
+    return max(idx) + 1 if idx else 0
+
+
+def dims(name):
+    """(NSP, NR, NREV, NPM) read from the emitted files themselves."""
+    d = ref_dir(name)
+    with open(os.path.join(d, "header.h")) as f:
+        nsp = int(re.search(r"#define NSP (\d+)", f.read()).group(1))
+    with open(os.path.join(d, "rxn_rates.c")) as f:
+        rr = f.read()
+    nr = _max_index(rr, "fwd_rxn_rates")
+    nrev = _max_index(rr, "rev_rxn_rates")
+    npm = 0
+    p = os.path.join(d, "rxn_rates_pres_mod.c")
+    if os.path.exists(p):
+        with open(p) as f:
+            npm = _max_index(f.read(), "pres_mod")
+    return nsp, nr, nrev, npm
+
+
+def _cc(args, cwd):
+    res = subprocess.run(args, cwd=cwd, capture_output=True, text=True)
+    return res.returncode, res.stdout + res.stderr
+
+
+def compile_ref(name, opt_parity="-O2", opt_fast="-O3"):
+    """Build libref.so (parity) and libref_omp.so (timed) for one name."""
+    d = ref_dir(name)
+    nsp, nr, nrev, npm = dims(name)
+    srcs = ["chem_utils.c", "rxn_rates.c", "spec_rates.c"]
+    if npm:
+        srcs.append("rxn_rates_pres_mod.c")
+    harness = os.path.join(HERE, "ref_harness.c")
+    defs = ["-DCRS_NSP=%d" % nsp, "-DCRS_NR=%d" % nr,
+            "-DCRS_NREV=%d" % nrev, "-DCRS_NPM=%d" % npm]
+    base = ["gcc", "-shared", "-fPIC", "-I", d] + defs
+    jobs = [(base + [opt_parity, "-ffp-contract=off", "-o", "libref.so"]
+             + srcs + [harness, "-lm"]),
+            (base + [opt_fast, "-fopenmp", "-o", "libref_omp.so"]
+             + srcs + [harness, "-lm"])]
+    procs = [subprocess.Popen(j, cwd=d, stdout=subprocess.PIPE,
+                              stderr=subprocess.STDOUT, text=True)
+             for j in jobs]
+    for j, p in zip(jobs, procs):
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("compile failed: %s\n%s" % (" ".join(j), out))
+    return os.path.join(d, "libref.so"), os.path.join(d, "libref_omp.so")
+
+
+def have_sources(name):
+    d = ref_dir(name)
+    return all(os.path.exists(os.path.join(d, f))
+               for f in ("chem_utils.c", "rxn_rates.c", "spec_rates.c",
+                         "header.h"))
+
+
+def main(argv):
+    if len(argv) < 3 or argv[1] not in ("generate", "compile", "all"):
+        print(__doc__)
+        return 2
+    sys.path.insert(0, REPO)
+    from create_rate_subs_gb300 import synth
+    for name in argv[2:]:
+        if argv[1] in ("generate", "all"):
+            mdir = os.path.join(REF_OUT, name, "_mech")
+            tmpdir = tempfile.mkdtemp(prefix="crs_mech_")
+            mp, tp = synth.write_mechanism(name, tmpdir)
+            generate(name, mp, tp)
+            os.makedirs(mdir, exist_ok=True)
+            shutil.copy(mp, mdir)
+            shutil.copy(tp, mdir)
+            shutil.rmtree(tmpdir)
+        if argv[1] in ("compile", "all"):
+            print(compile_ref(name))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv))

@@ -1,0 +1,181 @@
+"""ctypes front for the CPU oracle and the reference's emitted C.
+
+TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and bench.py's
+cpu_baseline / --impl reference legs import this module.  Nothing in the
+create_rate_subs_gb300 package may import it.
+
+* ``Oracle(blob)``: the table-driven restatement (crs_oracle.c), built with
+  ``gcc -O2 -ffp-contract=off -fopenmp`` into oracle/liboracle.so.
+* ``RefLib(name)``: the reference's emitted C for synthetic mechanism
+  ``name``, compiled by oracle/build_ref.py into oracle/_ref/<name>/.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = os.path.join(HERE, "crs_oracle.c")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64 = ctypes.c_int64
+
+
+def build(force=False):
+    """Compile liboracle.so if missing or older than its source."""
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC",
+           "-o", LIB + ".tmp", SRC, "-lm"]
+    subprocess.run(cmd, check=True, cwd=HERE)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+class _Batch(object):
+    """Common batch helpers over a C library with *_eval / *_wdot_omp."""
+
+    def _outs(self, n, want):
+        N, R, NREV, NPM = self.dims[:4]
+        shapes = dict(conc=N, fwd=R, rev=NREV, pm=NPM, wdot=N, misc=3)
+        return {k: (np.zeros((max(shapes[k], 1), n)) if k in want else None)
+                for k in shapes}
+
+    def eval(self, T, P, Y, want=("conc", "fwd", "rev", "pm", "wdot", "misc")):
+        """All stages for SoA states; Y has >= N-1 rows of n states."""
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = T.shape[0]
+        o = self._outs(n, want)
+        rc = self._eval(_i64(n), _ptr(T), _ptr(P), _ptr(Y), _i64(n),
+                        _ptr(o["conc"]), _ptr(o["fwd"]), _ptr(o["rev"]),
+                        _ptr(o["pm"]), _ptr(o["wdot"]), _ptr(o["misc"]))
+        if rc != 0:
+            raise RuntimeError("oracle eval failed (%d)" % rc)
+        N, R, NREV, NPM = self.dims[:4]
+        trim = dict(conc=N, fwd=R, rev=NREV, pm=NPM, wdot=N, misc=3)
+        return {k: v[:trim[k]] for k, v in o.items() if v is not None}
+
+    def wdot_omp(self, T, P, Y, nthreads=0, out=None):
+        n = T.shape[0]
+        if out is None:
+            out = np.zeros((self.dims[0], n))
+        used = self._omp(_i64(n), _ptr(T), _ptr(P), _ptr(Y), _i64(n),
+                         _ptr(out), ctypes.c_int(nthreads))
+        return out, used
+
+
+class Oracle(_Batch):
+    """Table-driven FP64 restatement of the emitted code."""
+
+    def __init__(self, blob):
+        build()
+        self.lib = ctypes.CDLL(LIB)
+        L = self.lib
+        L.oracle_load.argtypes = [ctypes.c_char_p, ctypes.c_size_t,
+                                  ctypes.POINTER(ctypes.c_void_p)]
+        L.oracle_free.argtypes = [ctypes.c_void_p]
+        L.oracle_dims.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_eval.argtypes = [ctypes.c_void_p, _i64, _dp, _dp, _dp, _i64,
+                                  _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_wdot_omp.argtypes = [ctypes.c_void_p, _i64, _dp, _dp, _dp,
+                                      _i64, _dp, ctypes.c_int]
+        h = ctypes.c_void_p()
+        rc = L.oracle_load(blob, len(blob), ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError("oracle_load failed (%d)" % rc)
+        self.h = h
+        d = (ctypes.c_int64 * 5)()
+        L.oracle_dims(h, d)
+        self.dims = tuple(int(x) for x in d)
+        self._eval = lambda *a: L.oracle_eval(self.h, *a)
+        self._omp = lambda *a: L.oracle_wdot_omp(self.h, *a)
+
+    def __del__(self):
+        try:
+            self.lib.oracle_free(self.h)
+        except Exception:
+            pass
+
+
+class RefLib(_Batch):
+    """The reference's emitted C for one synthetic mechanism."""
+
+    def __init__(self, name, omp=False):
+        d = os.path.join(HERE, "_ref", name)
+        path = os.path.join(d, "libref_omp.so" if omp else "libref.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = L = ctypes.CDLL(path)
+        L.ref_dims.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+        L.ref_eval.argtypes = [_i64, _dp, _dp, _dp, _i64, _dp, _dp, _dp, _dp,
+                               _dp, _dp]
+        L.ref_wdot_omp.argtypes = [_i64, _dp, _dp, _dp, _i64, _dp, ctypes.c_int]
+        dd = (ctypes.c_int64 * 4)()
+        L.ref_dims(dd)
+        self.dims = tuple(int(x) for x in dd)
+        self._eval = L.ref_eval
+        self._omp = L.ref_wdot_omp
+
+    @staticmethod
+    def available(name, omp=False):
+        return os.path.exists(os.path.join(
+            HERE, "_ref", name, "libref_omp.so" if omp else "libref.so"))
+
+
+def gross_scale(blob_tables, fwd, rev, pm):
+    """G[k, i] = sum_r |nu_kr| (|fwd_r| + |rev_r|) * pm_r: the scale of the
+    terms summed into wdot_k, used to normalise errors where fwd and rev
+    cancel."""
+    t = blob_tables
+    N = int(t["dims"][0])
+    R = int(t["dims"][1])
+    n = fwd.shape[1]
+    G = np.zeros((N, n))
+    for r in range(R):
+        j = t["rev_idx"][r]
+        p = t["pm_idx"][r]
+        g = np.abs(fwd[r]) + (np.abs(rev[j]) if j >= 0 else 0.0)
+        if p >= 0:
+            g = g * np.abs(pm[p])
+        for e in range(t["nu_ptr"][r], t["nu_ptr"][r + 1]):
+            G[t["nu_sp"][e]] += abs(t["nu_val"][e]) * g
+    return G
+
+
+def wdot_errors(w, w_ref, G):
+    """Error report for one result against an FP64 reference.
+
+    Returns dict with
+      ``scaled``: max |w - w_ref| / G (G = gross-rate scale), the headline
+                  relative error; it stays meaningful where fwd ~ rev;
+      ``scaled_rms``: RMS of the same ratio;
+      ``rel_wellcond``: max |w - w_ref| / |w_ref| over entries with
+                  |w_ref| >= 1e-3 G (cancellation at most 1000x);
+      ``rel_1e8``: the same over |w_ref| >= 1e-8 G.
+    Entries with G == 0 (species untouched) must match exactly.
+    """
+    w = np.asarray(w, dtype=np.float64)
+    d = np.abs(w - w_ref)
+    G = np.asarray(G)
+    zero = G == 0
+    if np.any(d[zero] != 0):
+        return dict(scaled=float("inf"), scaled_rms=float("inf"),
+                    rel_wellcond=float("inf"), rel_1e8=float("inf"))
+    Gs = np.where(zero, 1.0, G)
+    s = d / Gs
+    out = dict(scaled=float(np.max(s)) if s.size else 0.0,
+               scaled_rms=float(np.sqrt(np.mean(s ** 2))) if s.size else 0.0)
+    for key, thr in (("rel_wellcond", 1e-3), ("rel_1e8", 1e-8)):
+        m = (~zero) & (np.abs(w_ref) >= thr * G)
+        out[key] = float(np.max(d[m] / np.abs(w_ref[m]))) if np.any(m) else 0.0
+    return out
