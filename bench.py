@@ -1,0 +1,410 @@
+"""Throughput benchmark: species production rates wdot over many states.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {ours,reference}]
+
+Workload (one step): the fused wdot evaluation (eval_conc -> eval_rxn_rates
+-> get_rxn_pres_mod -> eval_spec_rates) of the seeded synthetic
+53-species / 325-reaction mechanism over 2^20 independent states per GPU,
+FP64 structure-of-arrays inputs resident in HBM (898 MB per step, larger
+than the 129 MB L2, so no flush is needed).  ``value`` is the plain FP64
+kernel's states/s; the same line carries the mixed-precision kernel at
+2^22 states with its measured error against the FP64 kernel, the
+end-to-end number through the C ABI from pinned host buffers, roofline
+fractions, clocks and the CPU baseline.
+
+``--impl reference`` times the reference's own emitted C for the same
+mechanism with OpenMP on every host core (compiled by
+oracle/build_ref.py; when it is not available, the CPU oracle port).
+Under torchrun every rank evaluates its own 2^20 states (weak scaling,
+no collective on the data path).
+"""
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_STATES = 1 << 20
+N_STATES_MIXED = 1 << 22
+MECH = "gri53"
+METRIC = "wdot states/s (53sp/325rxn) plain FP64 vs mixed & surrogate at stated rel err"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--states", type=int, default=N_STATES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _mechanism():
+    from create_rate_subs_gb300 import synth
+    from create_rate_subs_gb300.mechanism import Mechanism
+    d = tempfile.mkdtemp(prefix="crs_bench_")
+    mp, tp = synth.write_mechanism(MECH, d)
+    return Mechanism.from_chemkin(mp, tp)
+
+
+def _config(n):
+    return {"workload": "wdot, synthetic %s mechanism (53 species / 325 reactions: "
+                        "30 three-body, 25 Troe, 3 Lindemann, 2 SRI, 20 irreversible), "
+                        "plain FP64 kernel" % MECH,
+            "n_states_per_gpu": n, "layout": "SoA FP64 T,P,Y[52] in, wdot[53] out",
+            "l2": "inputs larger than L2 (%d MB per step)" % (n * 856 // 2**20)}
+
+
+def _cpu_sample(mech, n_target, seconds=12.0, threads=0):
+    """CPU baseline on a bounded sample: the reference's emitted C (OpenMP)
+    when built, else the oracle port.  Returns dict for cpu_baseline."""
+    from create_rate_subs_gb300 import synth
+    from oracle.oracle import Oracle, RefLib
+    if RefLib.available(MECH, omp=True):
+        lib, kind = RefLib(MECH, omp=True), "reference"
+    else:
+        lib, kind = Oracle(mech.blob), "port"
+    n = min(n_target, 1 << 16)
+    T, P, Y = synth.make_states(mech.n_species, n, seed=777)
+    lib.wdot_omp(T, P, Y, nthreads=threads)  # warm-up
+    done, t0, used = 0, time.perf_counter(), 1
+    while True:
+        _, used = lib.wdot_omp(T, P, Y, nthreads=threads)
+        done += n
+        el = time.perf_counter() - t0
+        if el > seconds or done >= n_target:
+            break
+    return {"value": done / el, "unit": "states/s", "cores": int(used), "kind": kind,
+            "sample": "%d states of the same workload (%d passes over %d seeded "
+                      "states), %.1f s wall" % (done, done // n, n, el)}
+
+
+class Clocks(object):
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile(prefix="crs_clk_", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.close()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 7:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        try:
+            sm = [float(r[0]) for r in rows]
+            mx = float(rows[0][1])
+        except ValueError:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _traffic_from_profiles(kernel):
+    """DRAM bytes per state from the committed ncu summary, if any."""
+    d = os.path.join(HERE, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".md"):
+            continue
+        with open(os.path.join(d, fn)) as f:
+            txt = f.read()
+        m = re.search(r"^dram_bytes_per_state\[%s\]:\s*([0-9.eE+-]+)" % re.escape(kernel),
+                      txt, re.M)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    mech = _mechanism()
+    # each of the K timed steps is one OpenMP pass over a bounded sample
+    from create_rate_subs_gb300 import synth
+    from oracle.oracle import Oracle, RefLib
+    if RefLib.available(MECH, omp=True):
+        lib, kind = RefLib(MECH, omp=True), "reference"
+    else:
+        lib, kind = Oracle(mech.blob), "port"
+    n = 1 << 16
+    T, P, Y = synth.make_states(mech.n_species, n, seed=778)
+    for _ in range(args.warmup):
+        lib.wdot_omp(T, P, Y)
+    t0 = time.perf_counter()
+    used = 1
+    for _ in range(args.steps):
+        _, used = lib.wdot_omp(T, P, Y)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    line = {"impl": "reference", "metric": METRIC,
+            "value": v, "unit": "states/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": _config(N_STATES),
+            "cpu_baseline": {"value": v, "unit": "states/s", "cores": int(used),
+                             "kind": kind,
+                             "sample": "%d states per step (seeded), %d timed steps"
+                                       % (n, args.steps)},
+            "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def _time_steps(fn, steps, warmup, stream, dist):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    return ms
+
+
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from create_rate_subs_gb300 import _lib, synth
+    from create_rate_subs_gb300.rates import RateSubs
+    from create_rate_subs_gb300.work import state_bytes, work
+
+    mech = _mechanism()
+    rs = RateSubs(mech)
+    lib = _lib.load()
+    N = mech.n_species
+    n = args.states
+    T, P, Y = synth.make_states(N, n, seed=1000 + rank)
+    dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[: N - 1].copy()))
+    out = torch.empty((N, n), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    import ctypes
+    pk = (ctypes.c_double * 4)()
+    _lib.check(lib.crs_probe_peaks(pk))
+    peaks = dict(fp64_fma_ops=pk[0], fp64_exp=pk[1], fp32_fma_ops=pk[2], sfu_ex2=pk[3])
+
+    modes = {}
+    for m in ("fp64", "fp64_strict", "mixed"):
+        try:
+            rs.wdot(dT[:1024], dP[:1024], dY[:, :1024], mode=m)
+            modes[m] = True
+        except _lib.CRSError as exc:
+            if exc.code != 4:
+                raise
+    plain = "fp64" if "fp64" in modes else "fp64_strict"
+
+    rs.reset_status()
+    clk = Clocks(local)
+    ms = _time_steps(lambda: rs.wdot(dT, dP, dY, plain, out=out), args.steps,
+                     args.warmup, stream, dist)
+    clocks = clk.stop()
+    value = n * world / (ms * 1e-3)
+
+    # accuracy of each mode against the strict FP64 kernel on a sub-sample
+    sub = min(n, 1 << 15)
+    ref = rs.wdot_stages(dT[:sub], dP[:sub], dY[:, :sub], "fp64_strict")
+    accuracy = {}
+    for m in modes:
+        w = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], m)
+        accuracy[m] = _scaled_error(mech.tables, w, ref)
+
+    # mixed precision at 2^22 states
+    mixed = None
+    if "mixed" in modes:
+        nm = N_STATES_MIXED
+        T2, P2, Y2 = synth.make_states(N, nm, seed=2000 + rank)
+        mT, mP, mY = (torch.from_numpy(a).cuda() for a in (T2, P2, Y2[: N - 1].copy()))
+        mo = torch.empty((N, nm), dtype=torch.float64, device="cuda")
+        msm = _time_steps(lambda: rs.wdot(mT, mP, mY, "mixed", out=mo), args.steps,
+                          args.warmup, stream, dist)
+        ms_plain22 = _time_steps(lambda: rs.wdot(mT, mP, mY, plain, out=mo),
+                                 max(2, args.steps // 2), 1, stream, dist)
+        mixed = {"states": nm, "value": nm * world / (msm * 1e-3), "unit": "states/s",
+                 "ms_per_step": msm, "plain_fp64_same_size": nm * world / (ms_plain22 * 1e-3),
+                 "speedup_vs_plain": ms_plain22 / msm, "error_vs_fp64": accuracy["mixed"]}
+        del mT, mP, mY, mo
+
+    # end to end through the C ABI with host buffers: H2D in, D2H out
+    hT = torch.from_numpy(T).pin_memory()
+    hP = torch.from_numpy(P).pin_memory()
+    hY = torch.from_numpy(Y[: N - 1].copy()).pin_memory()
+    hW = torch.empty((N, n), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        dT.copy_(hT, non_blocking=True)
+        dP.copy_(hP, non_blocking=True)
+        dY.copy_(hY, non_blocking=True)
+        _lib.check(lib.crs_wdot(rs.h, n, ctypes.c_void_p(dT.data_ptr()),
+                                ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(dY.data_ptr()),
+                                n, ctypes.c_void_p(out.data_ptr()), _lib.MODES[plain],
+                                ctypes.c_void_p(stream.cuda_stream)))
+        hW.copy_(out, non_blocking=True)
+    ms_e2e = _time_steps(e2e_step, max(3, args.steps // 2), 2, stream, dist)
+    h2d = (hT.numel() + hP.numel() + hY.numel()) * 8
+    d2h = hW.numel() * 8
+
+    flags, bad = rs.status()
+    wk = work(mech.tables)
+    per_state_s = ms * 1e-3 / n
+    t_roof = wk["flops"] / (2 * peaks["fp64_fma_ops"]) + wk["transcendentals"] / peaks["fp64_exp"]
+    eq_flops = wk["flops"] + wk["transcendentals"] * (2 * peaks["fp64_fma_ops"] / peaks["fp64_exp"])
+    achieved = eq_flops / per_state_s
+    peak = 2 * peaks["fp64_fma_ops"]
+    sb = state_bytes(N)
+    hbm_peak = None
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+        hbm_src = "of measured"
+    except (OSError, ValueError):
+        pass
+    if hbm_peak is None:
+        hbm_peak, hbm_src = 6800.0, "of fallback"
+    traffic = _traffic_from_profiles("fp64")
+    line = {
+        "metric": METRIC,
+        "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": _config(n), "plain_mode": plain,
+        "accuracy_vs_fp64_strict": accuracy,
+        "mixed": mixed,
+        "e2e": {"value": n * world / (ms_e2e * 1e-3), "unit": "states/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e, "path": "crs_wdot via ctypes, pinned host buffers"},
+        "gpu_launches": args.steps,
+        "roofline": {
+            "bound": "fp64", "unit": "GFLOP/s",
+            "achieved": achieved / 1e9, "peak": peak / 1e9, "frac": achieved / peak,
+            "peak_source": "measured in-run: FP64 FMA issue rate and CUDA exp() rate "
+                           "(crs_probe_peaks); transcendentals counted at exp()'s cost",
+            "per_state": {"flops": wk["flops"], "transcendentals": wk["transcendentals"],
+                          "roofline_ns": t_roof * 1e9, "measured_ns": per_state_s * 1e9},
+            "traffic": (traffic * n if traffic is not None else None),
+            "hbm": {"achieved_gbs": sb / per_state_s / 1e9, "peak_gbs": hbm_peak,
+                    "frac": sb / per_state_s / 1e9 / hbm_peak, "peak_note": hbm_src,
+                    "algorithmic_bytes_per_state": sb},
+        },
+        "peaks_measured": {k: v / 1e9 for k, v in peaks.items()},
+        "status": {"flags": flags, "nonfinite": bad},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = _cpu_sample(mech, n_target=n, seconds=12.0)
+    if rank == 0:
+        print(json.dumps(line, default=_jsonable))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def _jsonable(o):
+    if isinstance(o, (np.integer,)):
+        return int(o)
+    if isinstance(o, (np.floating,)):
+        return float(o)
+    raise TypeError(type(o))
+
+
+def _scaled_error(tables, w, ref):
+        """Error of a wdot result against the strict FP64 kernel's stages."""
+        import torch
+        t = tables
+        fwd, rev, pm, wr = (ref[k].double() for k in ("fwd", "rev", "pm", "wdot"))
+        R = int(t["dims"][1])
+        N = int(t["dims"][0])
+        rev_idx = torch.as_tensor(t["rev_idx"], device=fwd.device, dtype=torch.long)
+        pm_idx = torch.as_tensor(t["pm_idx"], device=fwd.device, dtype=torch.long)
+        g = fwd.abs().clone()
+        has_rev = rev_idx >= 0
+        if rev.shape[0]:
+            g[has_rev] += rev.abs()[rev_idx[has_rev]]
+        has_pm = pm_idx >= 0
+        if pm.shape[0]:
+            g[has_pm] *= pm.abs()[pm_idx[has_pm]]
+        M = torch.zeros((N, R), dtype=torch.float64, device=fwd.device)
+        for r in range(R):
+            for e in range(t["nu_ptr"][r], t["nu_ptr"][r + 1]):
+                M[t["nu_sp"][e], r] += abs(float(t["nu_val"][e]))
+        G = M @ g
+        d = (w.double() - wr).abs()
+        zero = G == 0
+        s = torch.where(zero, d, d / torch.where(zero, torch.ones_like(G), G))
+        mask = (~zero) & (wr.abs() >= 1e-3 * G)
+        rel = (d[mask] / wr.abs()[mask]).max().item() if mask.any() else 0.0
+        return {"scaled_max": s.max().item(), "scaled_rms": s.pow(2).mean().sqrt().item(),
+                "rel_max_wellcond": rel,
+                "normalisation": "|w-w64|/G, G_k=sum_r |nu_kr|(|fwd_r|+|rev_r|)pm_r; "
+                                 "rel over |w64|>=1e-3 G"}
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,89 @@
+"""ctypes binding of libcrs.so (include/crs.h).
+
+The library is built in-tree by ``create_rate_subs_gb300.build``.  Loading
+fails loudly when it is missing and cannot be built: there is no CPU
+fallback for the batched evaluation.
+"""
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+CRS_OK = 0
+ERRORS = {1: "bad argument", 2: "bad mechanism tables", 3: "CUDA error",
+          4: "unsupported", 5: "timeout", 6: "no mechanism bound"}
+
+MODES = {"fp64": 0, "fp64_strict": 1, "mixed": 2}
+
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_i32 = ctypes.c_int
+
+
+class CRSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("libcrs error %d (%s): %s" % (code, ERRORS.get(code, "?"), msg))
+        self.code = code
+
+
+def _sig(lib):
+    s = {
+        "crs_mech_load": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
+        "crs_mech_load_file": [ctypes.c_char_p, ctypes.POINTER(_vp)],
+        "crs_mech_free": [_vp],
+        "crs_mech_dims": [_vp, ctypes.POINTER(_i64)],
+        "crs_status": [_vp, _vp, ctypes.POINTER(ctypes.c_int32)],
+        "crs_status_reset": [_vp, _vp],
+        "crs_eval_conc_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp],
+        "crs_eval_rxn_rates_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp],
+        "crs_get_rxn_pres_mod_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
+        "crs_eval_spec_rates_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
+        "crs_wdot": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _i32, _vp],
+        "crs_wdot_stages": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
+                            _vp, _i32, _vp],
+        "crs_bind": [_vp],
+        "eval_conc": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
+        "eval_rxn_rates": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
+        "get_rxn_pres_mod": [ctypes.c_double, ctypes.c_double, _vp, _vp],
+        "eval_spec_rates": [_vp, _vp, _vp, _vp, _vp],
+    }
+    for name, args in s.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = None if name in ("eval_conc", "eval_rxn_rates",
+                                     "get_rxn_pres_mod", "eval_spec_rates") else ctypes.c_int
+    lib.crs_last_error.argtypes = []
+    lib.crs_last_error.restype = ctypes.c_char_p
+    return lib
+
+
+def load(build_if_missing=True):
+    """The loaded libcrs (built first if missing and nvcc is available)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise OSError("libcrs.so is not built (%s); run "
+                              "python -m create_rate_subs_gb300.build" % path)
+            _build.build()
+        _lib = _sig(ctypes.CDLL(path))
+        return _lib
+
+
+def check(rc):
+    if rc != CRS_OK:
+        msg = load().crs_last_error().decode(errors="replace")
+        raise CRSError(rc, msg)
+    return rc
+
+
+def last_error():
+    return load().crs_last_error().decode(errors="replace")

@@ -1,0 +1,591 @@
+// libcrs C ABI: mechanism loading, argument checking, kernel dispatch and
+// the reference's four per-state entry points.  See include/crs.h.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/crs.h"
+#include "crs_internal.cuh"
+
+namespace crs {
+cudaError_t launch_wdot_strict(const unsigned char *img, const ImgLayout &L,
+                               const Batch &b, int sm_count, int smem_optin,
+                               cudaStream_t s);
+cudaError_t launch_wdot_fp64(const unsigned char *img, const ImgLayout &L,
+                             const Batch &b, int sm_count, int smem_optin,
+                             cudaStream_t s);
+cudaError_t launch_wdot_mixed(const unsigned char *img, const ImgLayout &L,
+                              const Batch &b, int sm_count, int smem_optin,
+                              cudaStream_t s);
+cudaError_t launch_stage(int which, const unsigned char *img,
+                         const ImgLayout &L, const Batch &b, double *y_N,
+                         double *mw, double *rho, int sm_count, cudaStream_t s);
+// Derived tables appended to the image by the fast kernels' builders.
+bool build_fast_tables(const std::vector<unsigned char> &blob_img,
+                       const ImgLayout &L, std::vector<unsigned char> &extra,
+                       int base_offset, ImgLayout &out);
+}  // namespace crs
+
+struct crs_mech {
+  int device = 0;
+  int sm_count = 0;
+  int smem_optin = 0;
+  crs::ImgLayout L{};
+  unsigned char *d_img = nullptr;  // device table image
+  int32_t *d_status = nullptr;     // [0] flags, [1] non-finite count
+  std::vector<unsigned char> h_img;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(CRS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+struct Section {
+  uint32_t dtype;
+  uint64_t count, offset;
+};
+
+bool find_section(const unsigned char *b, size_t n, const char *name,
+                  Section &out) {
+  uint32_t nsec;
+  memcpy(&nsec, b + 12, 4);
+  if (16 + (size_t)nsec * 48 > n) return false;
+  for (uint32_t i = 0; i < nsec; ++i) {
+    const unsigned char *e = b + 16 + (size_t)i * 48;
+    char nm[25];
+    memcpy(nm, e, 24);
+    nm[24] = 0;
+    if (strcmp(nm, name) != 0) continue;
+    memcpy(&out.dtype, e + 24, 4);
+    memcpy(&out.count, e + 32, 8);
+    memcpy(&out.offset, e + 40, 8);
+    const size_t es = (out.dtype == 1 || out.dtype == 3) ? 8 : (out.dtype == 2 ? 4 : 1);
+    return out.offset + out.count * es <= n;
+  }
+  return false;
+}
+
+// Table sections copied into the device image: name, dtype, expected count
+// expressed through the dims (-1 = any).
+struct Want {
+  const char *name;
+  int *field;
+  uint32_t dtype;
+};
+
+int build_image(const unsigned char *b, size_t n, crs_mech *m) {
+  if (n < 16 || memcmp(b, "CRSMECH1", 8) != 0)
+    return fail(CRS_ERR_BLOB, "not a mechanism blob (bad magic)");
+  uint32_t ver;
+  memcpy(&ver, b + 8, 4);
+  if (ver != 1) return fail(CRS_ERR_BLOB, "unsupported blob version %u", ver);
+  Section s;
+  if (!find_section(b, n, "dims", s) || s.dtype != 3 || s.count < 5)
+    return fail(CRS_ERR_BLOB, "blob has no dims section");
+  int64_t dims[5];
+  memcpy(dims, b + s.offset, sizeof dims);
+  crs::ImgLayout &L = m->L;
+  L.N = (int)dims[0];
+  L.R = (int)dims[1];
+  L.NREV = (int)dims[2];
+  L.NPM = (int)dims[3];
+  L.NRATE = (int)dims[4];
+  if (L.N < 2 || L.R < 0 || L.NREV < 0 || L.NPM < 0 || L.NRATE < L.R)
+    return fail(CRS_ERR_BLOB, "bad dims");
+  Want want[] = {
+      {"sp_inv_mw", &L.inv_mw, 1}, {"rate_par", &L.rate_par, 1},
+      {"rx_nu", &L.rx_nu, 1}, {"px_nu", &L.px_nu, 1},
+      {"kc_tmid", &L.kc_tmid, 1}, {"kc_lo", &L.kc_lo, 1},
+      {"kc_hi", &L.kc_hi, 1}, {"kc_pref", &L.kc_pref, 1},
+      {"pm_eff_val", &L.pm_eff_val, 1}, {"pm_troe", &L.pm_troe, 1},
+      {"pm_sri", &L.pm_sri, 1}, {"nu_val", &L.nu_val, 1},
+      {"sp_tmid", &L.sp_tmid, 1}, {"sp_lo", &L.sp_lo, 1},
+      {"sp_hi", &L.sp_hi, 1}, {"kc_dnu", &L.kc_dnu, 1},
+      {"rate_kind", &L.rate_kind, 2}, {"rate_npow", &L.rate_npow, 2},
+      {"rx_ptr", &L.rx_ptr, 2}, {"rx_sp", &L.rx_sp, 2},
+      {"rx_nint", &L.rx_nint, 2}, {"px_ptr", &L.px_ptr, 2},
+      {"px_sp", &L.px_sp, 2}, {"px_nint", &L.px_nint, 2},
+      {"rev_idx", &L.rev_idx, 2}, {"kc_ptr", &L.kc_ptr, 2},
+      {"pm_idx", &L.pm_idx, 2}, {"pm_kind", &L.pm_kind, 2},
+      {"pm_form", &L.pm_form, 2}, {"pm_sp", &L.pm_sp, 2},
+      {"pm_eff_ptr", &L.pm_eff_ptr, 2}, {"pm_eff_sp", &L.pm_eff_sp, 2},
+      {"pm_k0", &L.pm_k0, 2}, {"pm_kinf", &L.pm_kinf, 2},
+      {"pm_troe_t2", &L.pm_troe_t2, 2}, {"pm_sri_de", &L.pm_sri_de, 2},
+      {"nu_ptr", &L.nu_ptr, 2}, {"nu_sp", &L.nu_sp, 2},
+  };
+  std::vector<unsigned char> &img = m->h_img;
+  img.clear();
+  std::vector<std::pair<const char *, Section>> got;
+  for (auto &w : want) {
+    if (!find_section(b, n, w.name, s))
+      return fail(CRS_ERR_BLOB, "blob lacks section %s", w.name);
+    if (s.dtype != w.dtype)
+      return fail(CRS_ERR_BLOB, "section %s has the wrong type", w.name);
+    const size_t es = w.dtype == 1 ? 8 : 4;
+    size_t off = (img.size() + 15) / 16 * 16;
+    img.resize(off + s.count * es + 16);  // +16: keeps empty sections valid
+    memcpy(img.data() + off, b + s.offset, s.count * es);
+    *w.field = (int)off;
+    got.emplace_back(w.name, s);
+  }
+  img.resize((img.size() + 15) / 16 * 16);
+  // Index sanity: every index stored in the tables must be in range, so
+  // that no kernel can read outside its tables or state columns.
+  const crs::Tab t = crs::make_tab(img.data(), L);
+  auto cnt = [&](const char *name) -> int64_t {
+    for (auto &g : got)
+      if (strcmp(g.first, name) == 0) return (int64_t)g.second.count;
+    return -1;
+  };
+  auto ptr_ok = [&](const int32_t *p, int len, int64_t total) {
+    if (p[0] != 0) return false;
+    for (int i = 0; i < len; ++i)
+      if (p[i + 1] < p[i]) return false;
+    return p[len] == total;
+  };
+  if (cnt("rate_par") != 4LL * L.NRATE || cnt("rate_kind") != L.NRATE ||
+      cnt("rx_ptr") != L.R + 1 || cnt("px_ptr") != L.R + 1 ||
+      cnt("nu_ptr") != L.R + 1 || cnt("rev_idx") != L.R ||
+      cnt("pm_idx") != L.R || cnt("kc_ptr") != L.NREV + 1 ||
+      cnt("pm_eff_ptr") != L.NPM + 1 || cnt("pm_kind") != L.NPM ||
+      cnt("sp_inv_mw") != L.N || cnt("sp_lo") != 7LL * L.N)
+    return fail(CRS_ERR_BLOB, "table sizes disagree with dims");
+  if (!ptr_ok(t.rx_ptr, L.R, cnt("rx_sp")) || !ptr_ok(t.px_ptr, L.R, cnt("px_sp")) ||
+      !ptr_ok(t.nu_ptr, L.R, cnt("nu_sp")) ||
+      !ptr_ok(t.kc_ptr, L.NREV, cnt("kc_tmid")) ||
+      !ptr_ok(t.pm_eff_ptr, L.NPM, cnt("pm_eff_sp")))
+    return fail(CRS_ERR_BLOB, "bad CSR pointers");
+  L.NKC = (int)cnt("kc_tmid");
+  auto in = [](int64_t v, int64_t lo, int64_t hi) { return v >= lo && v < hi; };
+  for (int64_t e = 0; e < cnt("rx_sp"); ++e)
+    if (!in(t.rx_sp[e], 0, L.N) || t.rx_nint[e] > 64) return fail(CRS_ERR_BLOB, "bad reactant");
+  for (int64_t e = 0; e < cnt("px_sp"); ++e)
+    if (!in(t.px_sp[e], 0, L.N) || t.px_nint[e] > 64) return fail(CRS_ERR_BLOB, "bad product");
+  for (int64_t e = 0; e < cnt("nu_sp"); ++e)
+    if (!in(t.nu_sp[e], 0, L.N)) return fail(CRS_ERR_BLOB, "bad nu species");
+  for (int64_t e = 0; e < cnt("pm_eff_sp"); ++e)
+    if (!in(t.pm_eff_sp[e], 0, L.N)) return fail(CRS_ERR_BLOB, "bad efficiency species");
+  int nrev = 0, npm = 0;
+  for (int r = 0; r < L.R; ++r) {
+    if (t.rev_idx[r] >= 0 && t.rev_idx[r] != nrev++) return fail(CRS_ERR_BLOB, "bad rev_idx");
+    if (t.pm_idx[r] >= 0 && t.pm_idx[r] != npm++) return fail(CRS_ERR_BLOB, "bad pm_idx");
+    if (!in(t.rate_kind[r], 0, 4) || t.rate_npow[r] > 64) return fail(CRS_ERR_BLOB, "bad rate");
+  }
+  if (nrev != L.NREV || npm != L.NPM) return fail(CRS_ERR_BLOB, "rev/pm counts disagree");
+  for (int p = 0; p < L.NPM; ++p) {
+    if (!in(t.pm_kind[p], 0, 3) || !in(t.pm_form[p], 0, 3) || t.pm_sp[p] >= L.N)
+      return fail(CRS_ERR_BLOB, "bad pres_mod entry");
+    if (t.pm_kind[p] != crs::PM_THD &&
+        (!in(t.pm_k0[p], 0, L.NRATE) || !in(t.pm_kinf[p], 0, L.NRATE)))
+      return fail(CRS_ERR_BLOB, "bad fall-off rate rows");
+  }
+  // Derived tables of the fast kernels.
+  std::vector<unsigned char> extra;
+  crs::ImgLayout L2 = L;
+  if (!crs::build_fast_tables(img, L, extra, (int)img.size(), L2))
+    return fail(CRS_ERR_BLOB, "could not derive fast tables");
+  img.insert(img.end(), extra.begin(), extra.end());
+  img.resize((img.size() + 15) / 16 * 16);
+  L = L2;
+  L.bytes = (int)img.size();
+  return CRS_OK;
+}
+
+bool check_device(const crs_mech *m) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != m->device) {
+    fail(CRS_ERR_ARG, "current device %d is not the mechanism's device %d",
+         dev, m->device);
+    return false;
+  }
+  return true;
+}
+
+int check_batch(const crs_mech *m, int64_t n, int64_t ld) {
+  if (!m) return fail(CRS_ERR_ARG, "mechanism is NULL");
+  if (n < 0) return fail(CRS_ERR_ARG, "n < 0");
+  if (ld < n) return fail(CRS_ERR_ARG, "ld < n");
+  if (!check_device(m)) return CRS_ERR_ARG;
+  return CRS_OK;
+}
+
+crs::Batch make_batch(const crs_mech *m, int64_t n, int64_t ld) {
+  crs::Batch b{};
+  b.n = n;
+  b.ld = ld;
+  b.status = m->d_status;
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *crs_last_error(void) { return g_err.c_str(); }
+
+int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
+  if (!blob || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  crs_mech *m = new crs_mech();
+  int rc = build_image(static_cast<const unsigned char *>(blob), nbytes, m);
+  if (rc != CRS_OK) {
+    delete m;
+    return rc;
+  }
+  cudaError_t e = cudaGetDevice(&m->device);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&m->smem_optin,
+                               cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device);
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_img, m->h_img.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->d_img, m->h_img.data(), m->h_img.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_status, 4 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, 4 * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    int r = cuda_fail(e, "crs_mech_load");
+    crs_mech_free(m);
+    return r;
+  }
+  // reserve the static __shared__ mbarrier and a little slack
+  m->smem_optin -= 64;
+  *out = m;
+  return CRS_OK;
+}
+
+int crs_mech_load_file(const char *path, crs_mech **out) {
+  if (!path || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return fail(CRS_ERR_ARG, "cannot open %s", path);
+  std::vector<char> buf((std::istreambuf_iterator<char>(f)),
+                        std::istreambuf_iterator<char>());
+  return crs_mech_load(buf.data(), buf.size(), out);
+}
+
+int crs_mech_free(crs_mech *m) {
+  if (!m) return CRS_OK;
+  if (m->d_img) cudaFree(m->d_img);
+  if (m->d_status) cudaFree(m->d_status);
+  delete m;
+  return CRS_OK;
+}
+
+int crs_mech_dims(const crs_mech *m, int64_t out[5]) {
+  if (!m || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  out[0] = m->L.N;
+  out[1] = m->L.R;
+  out[2] = m->L.NREV;
+  out[3] = m->L.NPM;
+  out[4] = m->L.NRATE;
+  return CRS_OK;
+}
+
+int crs_status(const crs_mech *m, void *stream, int32_t out[2]) {
+  if (!m || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(out, m->d_status, 2 * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_status");
+}
+
+int crs_status_reset(const crs_mech *m, void *stream) {
+  if (!m) return fail(CRS_ERR_ARG, "NULL argument");
+  cudaError_t e = cudaMemsetAsync(m->d_status, 0, 2 * sizeof(int32_t),
+                                  static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_status_reset");
+}
+
+int crs_eval_conc_batch(const crs_mech *m, int64_t n, const double *T,
+                        const double *P, const double *Y, int64_t ld,
+                        double *y_N, double *mw_avg, double *rho, double *conc,
+                        void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !P || !Y || !conc) return fail(CRS_ERR_ARG, "NULL array");
+  crs::Batch b = make_batch(m, n, ld);
+  b.T = T; b.P = P; b.Y = Y; b.conc = conc;
+  cudaError_t e = crs::launch_stage(0, m->d_img, m->L, b, y_N, mw_avg, rho,
+                                    m->sm_count, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "eval_conc launch");
+}
+
+int crs_eval_rxn_rates_batch(const crs_mech *m, int64_t n, const double *T,
+                             const double *P, const double *C, int64_t ld,
+                             double *fwd, double *rev, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !P || !C || !fwd || (m->L.NREV > 0 && !rev))
+    return fail(CRS_ERR_ARG, "NULL array");
+  crs::Batch b = make_batch(m, n, ld);
+  b.T = T; b.P = P; b.conc = const_cast<double *>(C); b.fwd = fwd; b.rev = rev;
+  cudaError_t e = crs::launch_stage(1, m->d_img, m->L, b, nullptr, nullptr,
+                                    nullptr, m->sm_count, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "eval_rxn_rates launch");
+}
+
+int crs_get_rxn_pres_mod_batch(const crs_mech *m, int64_t n, const double *T,
+                               const double *P, const double *C, int64_t ld,
+                               double *pres_mod, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0 || m->L.NPM == 0) return CRS_OK;
+  if (!T || !P || !C || !pres_mod) return fail(CRS_ERR_ARG, "NULL array");
+  crs::Batch b = make_batch(m, n, ld);
+  b.T = T; b.P = P; b.conc = const_cast<double *>(C); b.pm = pres_mod;
+  cudaError_t e = crs::launch_stage(2, m->d_img, m->L, b, nullptr, nullptr,
+                                    nullptr, m->sm_count, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "get_rxn_pres_mod launch");
+}
+
+int crs_eval_spec_rates_batch(const crs_mech *m, int64_t n, const double *fwd,
+                              const double *rev, const double *pres_mod,
+                              int64_t ld, double *wdot, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!fwd || !wdot || (m->L.NREV > 0 && !rev) || (m->L.NPM > 0 && !pres_mod))
+    return fail(CRS_ERR_ARG, "NULL array");
+  crs::Batch b = make_batch(m, n, ld);
+  b.fwd = const_cast<double *>(fwd); b.rev = const_cast<double *>(rev);
+  b.pm = const_cast<double *>(pres_mod); b.wdot = wdot;
+  cudaError_t e = crs::launch_stage(3, m->d_img, m->L, b, nullptr, nullptr,
+                                    nullptr, m->sm_count, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "eval_spec_rates launch");
+}
+
+int crs_wdot_stages(const crs_mech *m, int64_t n, const double *T,
+                    const double *P, const double *Y, int64_t ld, double *wdot,
+                    double *conc, double *fwd, double *rev, double *pres_mod,
+                    int mode, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !P || !Y || !wdot) return fail(CRS_ERR_ARG, "NULL array");
+  crs::Batch b = make_batch(m, n, ld);
+  b.T = T; b.P = P; b.Y = Y; b.wdot = wdot;
+  b.conc = conc; b.fwd = fwd; b.rev = rev; b.pm = pres_mod;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  switch (mode) {
+    case CRS_MODE_FP64_STRICT:
+      e = crs::launch_wdot_strict(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64:
+      e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED:
+      e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    default:
+      return fail(CRS_ERR_ARG, "unknown mode %d", mode);
+  }
+  if (e == cudaErrorNotSupported)
+    return fail(CRS_ERR_UNSUPPORTED, "mode %d is not available for this mechanism", mode);
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_wdot launch");
+}
+
+int crs_wdot(const crs_mech *m, int64_t n, const double *T, const double *P,
+             const double *Y, int64_t ld, double *wdot, int mode, void *stream) {
+  return crs_wdot_stages(m, n, T, P, Y, ld, wdot, nullptr, nullptr, nullptr,
+                         nullptr, mode, stream);
+}
+
+}  // extern "C"
+
+// ---- per-state drop-in ---------------------------------------------------
+namespace {
+struct Bound {
+  std::mutex mu;
+  const crs_mech *m = nullptr;
+  double *d = nullptr;  // device scratch for one state
+  size_t words = 0;
+};
+Bound g_bound;
+
+void fill_nan(double *p, int n) {
+  if (!p) return;
+  for (int i = 0; i < n; ++i) p[i] = __builtin_nan("");
+}
+
+// Device scratch for one state: T, P, y/C [N], fwd [R], rev [R_rev],
+// pm [N_pm], wdot [N], y_N, mw, rho.
+struct One {
+  double *T, *P, *C, *fwd, *rev, *pm, *w, *misc;
+};
+One layout(const crs_mech *m, double *d) {
+  One o;
+  const crs::ImgLayout &L = m->L;
+  o.T = d;
+  o.P = d + 1;
+  o.C = d + 2;
+  o.fwd = o.C + L.N;
+  o.rev = o.fwd + L.R;
+  o.pm = o.rev + (L.NREV > 0 ? L.NREV : 1);
+  o.w = o.pm + (L.NPM > 0 ? L.NPM : 1);
+  o.misc = o.w + L.N;
+  return o;
+}
+}  // namespace
+
+extern "C" {
+
+int crs_bind(const crs_mech *m) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  if (g_bound.d) {
+    cudaFree(g_bound.d);
+    g_bound.d = nullptr;
+  }
+  g_bound.m = m;
+  if (!m) return CRS_OK;
+  const crs::ImgLayout &L = m->L;
+  g_bound.words = 2 + 2 * (size_t)L.N + L.R + (L.NREV + 1) + (L.NPM + 1) + 3;
+  cudaError_t e = cudaMalloc(&g_bound.d, g_bound.words * sizeof(double));
+  if (e != cudaSuccess) {
+    g_bound.m = nullptr;
+    return cuda_fail(e, "crs_bind");
+  }
+  return CRS_OK;
+}
+
+void eval_conc(const double T, const double pres, const double *y, double *y_N,
+               double *mw_avg, double *rho, double *conc) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "eval_conc: no mechanism bound (crs_bind)");
+    return;
+  }
+  One o = layout(m, g_bound.d);
+  const int N = m->L.N;
+  double tp[2] = {T, pres};
+  crs::Batch b = make_batch(m, 1, 1);
+  b.T = o.T; b.P = o.P; b.Y = o.C; b.conc = o.w;
+  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(o.C, y, (N - 1) * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = crs::launch_stage(0, m->d_img, m->L, b, o.misc, o.misc + 1, o.misc + 2,
+                          m->sm_count, 0);
+  double misc[3];
+  if (e == cudaSuccess)
+    e = cudaMemcpy(conc, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(misc, o.misc, sizeof misc, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "eval_conc");
+    fill_nan(conc, N);
+    misc[0] = misc[1] = misc[2] = __builtin_nan("");
+  }
+  *y_N = misc[0];
+  *mw_avg = misc[1];
+  *rho = misc[2];
+}
+
+void eval_rxn_rates(const double T, const double pres, const double *C,
+                    double *fwd_rxn_rates, double *rev_rxn_rates) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "eval_rxn_rates: no mechanism bound (crs_bind)");
+    return;
+  }
+  One o = layout(m, g_bound.d);
+  const crs::ImgLayout &L = m->L;
+  double tp[2] = {T, pres};
+  crs::Batch b = make_batch(m, 1, 1);
+  b.T = o.T; b.P = o.P; b.conc = o.C; b.fwd = o.fwd; b.rev = o.rev;
+  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(o.C, C, L.N * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = crs::launch_stage(1, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(fwd_rxn_rates, o.fwd, L.R * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && L.NREV > 0)
+    e = cudaMemcpy(rev_rxn_rates, o.rev, L.NREV * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "eval_rxn_rates");
+    fill_nan(fwd_rxn_rates, L.R);
+    fill_nan(rev_rxn_rates, L.NREV);
+  }
+}
+
+void get_rxn_pres_mod(const double T, const double pres, const double *C,
+                      double *pres_mod) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "get_rxn_pres_mod: no mechanism bound (crs_bind)");
+    return;
+  }
+  const crs::ImgLayout &L = m->L;
+  if (L.NPM == 0) return;
+  One o = layout(m, g_bound.d);
+  double tp[2] = {T, pres};
+  crs::Batch b = make_batch(m, 1, 1);
+  b.T = o.T; b.P = o.P; b.conc = o.C; b.pm = o.pm;
+  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(o.C, C, L.N * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = crs::launch_stage(2, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(pres_mod, o.pm, L.NPM * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "get_rxn_pres_mod");
+    fill_nan(pres_mod, L.NPM);
+  }
+}
+
+void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
+                     const double *pres_mod, double *sp_rates, double *dy_N) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "eval_spec_rates: no mechanism bound (crs_bind)");
+    return;
+  }
+  const crs::ImgLayout &L = m->L;
+  One o = layout(m, g_bound.d);
+  crs::Batch b = make_batch(m, 1, 1);
+  b.fwd = o.fwd; b.rev = o.rev; b.pm = o.pm; b.wdot = o.w;
+  cudaError_t e = cudaMemcpy(o.fwd, fwd_rates, L.R * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && L.NREV > 0)
+    e = cudaMemcpy(o.rev, rev_rates, L.NREV * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && L.NPM > 0)
+    e = cudaMemcpy(o.pm, pres_mod, L.NPM * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = crs::launch_stage(3, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
+  std::vector<double> w(L.N);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(w.data(), o.w, L.N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "eval_spec_rates");
+    fill_nan(w.data(), L.N);
+  }
+  for (int k = 0; k < L.N - 1; ++k) sp_rates[k] = w[k];
+  *dy_N = w[L.N - 1];
+}
+
+}  // extern "C"

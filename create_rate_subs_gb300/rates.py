@@ -1,0 +1,196 @@
+"""Batched evaluation of the reference's rate functions on the GPU.
+
+``RateSubs`` is the Python face of libcrs.  It mirrors the four functions
+create_rate_subs emits (rate_subs.py:1297-1299, 287-290, 761-763,
+1124-1127) -- same names, same arguments, same units -- but each call
+evaluates a whole batch of states held on the GPU:
+
+* ``eval_conc(T, P, Y)``          -> (y_N, mw_avg, rho, conc)
+* ``eval_rxn_rates(T, P, C)``     -> (fwd, rev)
+* ``get_rxn_pres_mod(T, P, C)``   -> pres_mod
+* ``eval_spec_rates(fwd, rev, pres_mod)`` -> wdot (row N-1 = dy_N)
+* ``wdot(T, P, Y, mode)``         -> the fused hot path
+
+Arrays are torch CUDA tensors in structure-of-arrays layout: ``T`` and ``P``
+have shape (n,), ``Y`` shape (N-1, n) or (N, n) (only the first N-1 rows
+are read), per-species / per-reaction outputs shape (rows, n).  Calls are
+ordered on torch's current CUDA stream.
+
+``wdot_host`` runs the same evaluation from host (numpy) arrays, copies
+included.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .mechanism import Mechanism
+
+__all__ = ["RateSubs"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class RateSubs(object):
+    """A mechanism staged on the current CUDA device."""
+
+    def __init__(self, mech, device=None):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("RateSubs needs a CUDA device")
+        self.lib = _lib.load()
+        self.mech = mech if isinstance(mech, Mechanism) else None
+        blob = mech.blob if isinstance(mech, Mechanism) else bytes(mech)
+        self.device = torch.device("cuda", torch.cuda.current_device()
+                                   if device is None else device)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.crs_mech_load(blob, len(blob), ctypes.byref(h)))
+        self.h = h
+        d = (ctypes.c_int64 * 5)()
+        _lib.check(self.lib.crs_mech_dims(h, d))
+        self.n_species, self.n_reactions, self.n_rev, self.n_pdep, _ = (int(x) for x in d)
+
+    @classmethod
+    def from_chemkin(cls, mech_filename, therm_filename=None, last_spec=None):
+        return cls(Mechanism.from_chemkin(mech_filename, therm_filename, last_spec))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.crs_mech_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- helpers ---------------------------------------------------------
+    def _stream(self):
+        return ctypes.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
+
+    def _check_states(self, T, P, Y=None, rows=None):
+        torch = _torch()
+        for name, a in (("T", T), ("P", P)):
+            if a.dtype != torch.float64 or a.dim() != 1 or not a.is_cuda:
+                raise ValueError("%s must be a 1-D float64 CUDA tensor" % name)
+            if a.stride(0) != 1:
+                raise ValueError("%s must be contiguous" % name)
+        n = T.shape[0]
+        if P.shape[0] != n:
+            raise ValueError("T and P differ in length")
+        ld = n
+        if Y is not None:
+            if Y.dtype != torch.float64 or Y.dim() != 2 or not Y.is_cuda:
+                raise ValueError("Y must be a 2-D float64 CUDA tensor (species, n)")
+            if Y.shape[1] != n or Y.stride(1) != 1:
+                raise ValueError("Y must be (species, n) with unit state stride")
+            if Y.shape[0] < (rows if rows is not None else self.n_species - 1):
+                raise ValueError("Y has too few species rows")
+            ld = Y.stride(0)
+        return n, ld
+
+    def _out(self, rows, n):
+        torch = _torch()
+        return torch.empty((max(rows, 0), n), dtype=torch.float64, device=self.device)
+
+    # -- the reference's functions, batched ------------------------------
+    def eval_conc(self, T, P, Y):
+        n, ld = self._check_states(T, P, Y)
+        torch = _torch()
+        conc = self._out(self.n_species, n)
+        if ld != n:
+            Y = Y[: self.n_species - 1].contiguous()
+        misc = torch.empty((3, n), dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.crs_eval_conc_batch(
+            self.h, n, _ptr(T), _ptr(P), _ptr(Y), n, _ptr(misc[0]), _ptr(misc[1]),
+            _ptr(misc[2]), _ptr(conc), self._stream()))
+        return misc[0], misc[1], misc[2], conc
+
+    def eval_rxn_rates(self, T, P, C):
+        n, _ = self._check_states(T, P, C, rows=self.n_species)
+        C = C.contiguous()
+        fwd = self._out(self.n_reactions, n)
+        rev = self._out(self.n_rev, n)
+        _lib.check(self.lib.crs_eval_rxn_rates_batch(
+            self.h, n, _ptr(T), _ptr(P), _ptr(C), n, _ptr(fwd),
+            _ptr(rev) if self.n_rev else None, self._stream()))
+        return fwd, rev
+
+    def get_rxn_pres_mod(self, T, P, C):
+        n, _ = self._check_states(T, P, C, rows=self.n_species)
+        C = C.contiguous()
+        pm = self._out(self.n_pdep, n)
+        if self.n_pdep:
+            _lib.check(self.lib.crs_get_rxn_pres_mod_batch(
+                self.h, n, _ptr(T), _ptr(P), _ptr(C), n, _ptr(pm), self._stream()))
+        return pm
+
+    def eval_spec_rates(self, fwd, rev, pres_mod):
+        n = fwd.shape[1]
+        fwd = fwd.contiguous()
+        rev = rev.contiguous() if rev is not None else None
+        pres_mod = pres_mod.contiguous() if pres_mod is not None else None
+        w = self._out(self.n_species, n)
+        _lib.check(self.lib.crs_eval_spec_rates_batch(
+            self.h, n, _ptr(fwd), _ptr(rev) if self.n_rev else None,
+            _ptr(pres_mod) if self.n_pdep else None, n, _ptr(w), self._stream()))
+        return w
+
+    # -- fused hot path ----------------------------------------------------
+    def wdot(self, T, P, Y, mode="fp64", out=None):
+        """wdot (N, n) for every state, one launch."""
+        n, ld = self._check_states(T, P, Y)
+        if out is None:
+            out = self._out(self.n_species, n)
+            ldw = n
+        else:
+            ldw = out.stride(0)
+        if ldw != ld:
+            Y = Y[: self.n_species - 1].contiguous() if ld != n else Y
+            if ldw != n:
+                raise ValueError("out must be (species, n) contiguous")
+            ld = n
+        _lib.check(self.lib.crs_wdot(self.h, n, _ptr(T), _ptr(P), _ptr(Y), ld,
+                                     _ptr(out), _lib.MODES[mode], self._stream()))
+        return out
+
+    def wdot_stages(self, T, P, Y, mode="fp64_strict"):
+        """wdot plus conc, fwd, rev, pres_mod from the fused kernel."""
+        n, ld = self._check_states(T, P, Y)
+        if ld != n:
+            Y = Y[: self.n_species - 1].contiguous()
+        o = dict(wdot=self._out(self.n_species, n), conc=self._out(self.n_species, n),
+                 fwd=self._out(self.n_reactions, n), rev=self._out(self.n_rev, n),
+                 pm=self._out(self.n_pdep, n))
+        _lib.check(self.lib.crs_wdot_stages(
+            self.h, n, _ptr(T), _ptr(P), _ptr(Y), n, _ptr(o["wdot"]), _ptr(o["conc"]),
+            _ptr(o["fwd"]), _ptr(o["rev"]) if self.n_rev else None,
+            _ptr(o["pm"]) if self.n_pdep else None, _lib.MODES[mode], self._stream()))
+        return o
+
+    def wdot_host(self, T, P, Y, mode="fp64"):
+        """wdot from host arrays: copy in, evaluate, copy out (numpy)."""
+        torch = _torch()
+        t = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
+             for a in (T, P, Y)]
+        w = self.wdot(t[0], t[1], t[2], mode)
+        return w.cpu().numpy()
+
+    def status(self):
+        """(flag bits, count of non-finite wdot values) since the last reset."""
+        out = (ctypes.c_int32 * 2)()
+        _lib.check(self.lib.crs_status(self.h, self._stream(), out))
+        return int(out[0]), int(out[1])
+
+    def reset_status(self):
+        _lib.check(self.lib.crs_status_reset(self.h, self._stream()))

@@ -1,0 +1,83 @@
+"""Algorithmic cost of one state, counted in the emitted code's own terms.
+
+Used for roofline fractions.  ``state_bytes``: the minimum HBM traffic of
+one state at FP64 -- read T, P and N-1 mass fractions, write N production
+rates.  ``work``: floating-point operations and transcendental calls that
+the reference's emitted C performs for one state (rate_subs.py:283-1391):
+eval_conc, eval_rxn_rates, get_rxn_pres_mod, eval_spec_rates.  An FMA
+counts 2 flops, a divide 1, a call to exp/log/log10/pow one transcendental.
+"""
+
+from .tables import (FORM_SRI, FORM_TROE, PM_THD, RATE_CONST, RATE_EXP,
+                     RATE_NEGEXP)
+
+__all__ = ["state_bytes", "work"]
+
+
+def state_bytes(n_species, elem_bytes=8):
+    return elem_bytes * (2 + (n_species - 1)) + elem_bytes * n_species
+
+
+def _rate(kind, npow):
+    """(flops, transcendentals) of one rxn_rate_const expression."""
+    if kind == RATE_CONST:
+        return 0, 0
+    if kind == RATE_EXP:
+        return 4, 1          # b*logT, +, Ta/T, -, exp
+    if kind == RATE_NEGEXP:
+        return 4, 1          # b*logT, Ta/T, -, exp, A*
+    return npow, 0
+
+
+def work(tables):
+    """dict(flops=..., transcendentals=..., exps=...) for one state."""
+    t = tables
+    N, R = int(t["dims"][0]), int(t["dims"][1])
+    NPM = int(t["dims"][3])
+    flops = 5 * N            # eval_conc
+    trans = 1                # log(T) in eval_rxn_rates
+    for r in range(R):
+        f, x = _rate(int(t["rate_kind"][r]), int(t["rate_npow"][r]))
+        flops += f
+        trans += x
+        nr = sum(max(int(v), 1) for v in t["rx_nint"][t["rx_ptr"][r]:t["rx_ptr"][r + 1]])
+        flops += nr          # concentration products and the kf factor
+        j = int(t["rev_idx"][r])
+        if j >= 0:
+            ng = int(t["kc_ptr"][j + 1] - t["kc_ptr"][j])
+            flops += 13 * ng + (ng - 1) + 1   # Kc polynomial(s), prefactor
+            trans += 1                        # exp(Kc)
+            npr = sum(max(int(v), 1) for v in t["px_nint"][t["px_ptr"][r]:t["px_ptr"][r + 1]])
+            flops += npr + 1                  # products, * kf, / Kc
+            flops += 1                        # fwd - rev
+        nnz = int(t["nu_ptr"][r + 1] - t["nu_ptr"][r])
+        p = int(t["pm_idx"][r])
+        for e in range(t["nu_ptr"][r], t["nu_ptr"][r + 1]):
+            flops += 1 + (abs(t["nu_val"][e]) != 1.0) + (p >= 0)
+        del nnz
+    if NPM:
+        trans += 1
+        flops += 2               # m = P / (RU * T)
+    for p in range(NPM):
+        ne = int(t["pm_eff_ptr"][p + 1] - t["pm_eff_ptr"][p])
+        if int(t["pm_kind"][p]) == PM_THD:
+            flops += 2 * ne
+            continue
+        if int(t["pm_sp"][p]) < 0:
+            flops += 2 * ne
+        for row in (int(t["pm_k0"][p]), int(t["pm_kinf"][p])):
+            f, x = _rate(int(t["rate_kind"][row]), int(t["rate_npow"][row]))
+            flops += f
+            trans += x
+        flops += 2               # Pr
+        form = int(t["pm_form"][p])
+        if form == FORM_TROE:
+            has2 = int(t["pm_troe_t2"][p])
+            flops += 5 + 2 * has2 + 3 + 4 + 5
+            trans += 2 + has2 + 3 + 1      # exps, 3 log10, pow(10, .)
+        elif form == FORM_SRI:
+            de = int(t["pm_sri_de"][p])
+            flops += 7 + 2 * de
+            trans += 2 + 2 + 1 + de        # exps, 2 log10, pow, pow(T, e)
+        flops += 3
+    return dict(flops=int(flops), transcendentals=int(trans))

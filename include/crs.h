@@ -1,0 +1,143 @@
+/*
+ * crs.h -- C ABI of libcrs, the sm_103a (GB300) evaluation library behind
+ * create_rate_subs_gb300.
+ *
+ * The reference (kyleniemeyer/create_rate_subs) emits, per mechanism, four
+ * per-state C functions that an integrator calls once per thermochemical
+ * state.  libcrs keeps those four signatures (bottom of this file) and adds
+ * batched, stream-ordered entry points over millions of states held in
+ * device memory in structure-of-arrays layout.
+ *
+ * Conventions for the batched entry points
+ *  - every array argument is a DEVICE pointer owned by the caller;
+ *  - SoA layout: entry k of state i lives at [k*ld + i]; ld >= n;
+ *  - Y holds the first N-1 mass fractions (species order of the mechanism);
+ *    the last one is implied, as in the reference's eval_conc;
+ *  - calls are asynchronous on `stream` (a cudaStream_t, NULL = legacy
+ *    default stream) and do not synchronise;
+ *  - return 0 on success or a CRS_ERR_* code; crs_last_error() describes
+ *    the last failure of the calling thread;
+ *  - a crs_mech is immutable after crs_mech_load and may be used from
+ *    several host threads at once; each handle owns one device status word
+ *    that concurrent launches on the same handle share.
+ * Units are the reference's: T [K], P [Pa], C [kmol/m^3], rates
+ * [kmol/(m^3 s)].
+ */
+#ifndef CRS_H
+#define CRS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct crs_mech crs_mech;
+
+#define CRS_OK 0
+#define CRS_ERR_ARG 1         /* NULL pointer, n < 0, ld < n, bad mode */
+#define CRS_ERR_BLOB 2        /* malformed mechanism tables */
+#define CRS_ERR_CUDA 3        /* CUDA runtime error (text in crs_last_error) */
+#define CRS_ERR_UNSUPPORTED 4 /* mode not available for this mechanism */
+#define CRS_ERR_TIMEOUT 5     /* a bounded device or host wait expired */
+#define CRS_ERR_NOMECH 6      /* per-state call without crs_bind */
+
+/* Evaluation modes of crs_wdot. */
+#define CRS_MODE_FP64 0        /* FP64 throughout; <=1e-12 of the reference */
+#define CRS_MODE_FP64_STRICT 1 /* FP64 in the reference's operation order */
+#define CRS_MODE_MIXED 2       /* FP32 bulk, FP64 Kc exponent/net rate/sum */
+
+/* ---- mechanism tables ------------------------------------------------ */
+
+/* Load the table blob written by create_rate_subs_gb300 (tables.pack; the
+ * 'gb300' CLI target writes it to out/mech.crs) and stage it on the current
+ * device.  Replaces the constants the reference bakes into its emitted
+ * code (rate_subs.py:226-1391). */
+int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out);
+int crs_mech_load_file(const char *path, crs_mech **out);
+int crs_mech_free(crs_mech *mech);
+/* out[0..4] = species, reactions, reversible reactions, pres_mod entries,
+ * rate-constant rows. */
+int crs_mech_dims(const crs_mech *mech, int64_t out[5]);
+const char *crs_last_error(void);
+/* Non-finite outputs and device-wait timeouts recorded since the last
+ * crs_status_reset on this handle: out[0] = flag bits (1 = table staging
+ * timed out), out[1] = count of non-finite wdot values.  Synchronises
+ * `stream`. */
+int crs_status(const crs_mech *mech, void *stream, int32_t out[2]);
+int crs_status_reset(const crs_mech *mech, void *stream);
+
+/* ---- batched stages (reference functions, many states) ---------------- */
+
+/* eval_conc over n states (rate_subs.py:1295-1391).  y_N, mw_avg, rho may
+ * be NULL; conc is [N][ld]. */
+int crs_eval_conc_batch(const crs_mech *mech, int64_t n, const double *T,
+                        const double *P, const double *Y, int64_t ld,
+                        double *y_N, double *mw_avg, double *rho,
+                        double *conc, void *stream);
+/* eval_rxn_rates (rate_subs.py:283-704): fwd [R][ld], rev [R_rev][ld]. */
+int crs_eval_rxn_rates_batch(const crs_mech *mech, int64_t n, const double *T,
+                             const double *P, const double *C, int64_t ld,
+                             double *fwd, double *rev, void *stream);
+/* get_rxn_pres_mod (rate_subs.py:757-1073): pres_mod [N_pm][ld]. */
+int crs_get_rxn_pres_mod_batch(const crs_mech *mech, int64_t n,
+                               const double *T, const double *P,
+                               const double *C, int64_t ld, double *pres_mod,
+                               void *stream);
+/* eval_spec_rates (rate_subs.py:1121-1235): wdot [N][ld] (row N-1 is the
+ * reference's *dy_N). */
+int crs_eval_spec_rates_batch(const crs_mech *mech, int64_t n,
+                              const double *fwd, const double *rev,
+                              const double *pres_mod, int64_t ld, double *wdot,
+                              void *stream);
+
+/* ---- fused hot path --------------------------------------------------- */
+
+/* wdot [N][ld] for n states in one launch: eval_conc -> eval_rxn_rates ->
+ * get_rxn_pres_mod -> eval_spec_rates fused, intermediates on chip. */
+int crs_wdot(const crs_mech *mech, int64_t n, const double *T,
+             const double *P, const double *Y, int64_t ld, double *wdot,
+             int mode, void *stream);
+/* crs_wdot that also writes the intermediates (any may be NULL): conc
+ * [N][ld], fwd [R][ld], rev [R_rev][ld], pres_mod [N_pm][ld].  For
+ * per-stage parity checks. */
+int crs_wdot_stages(const crs_mech *mech, int64_t n, const double *T,
+                    const double *P, const double *Y, int64_t ld,
+                    double *wdot, double *conc, double *fwd, double *rev,
+                    double *pres_mod, int mode, void *stream);
+
+/* ---- measurement helper (no counterpart in the reference) ------------- */
+
+/* Issue-rate probes of the current device, operations per second:
+ * out[0] FP64 FMA, out[1] CUDA double exp(), out[2] FP32 FMA, out[3] SFU
+ * ex2.approx.  The roofline denominators of the FP64 and mixed kernels. */
+int crs_probe_peaks(double out[4]);
+
+/* ---- per-state drop-in (the reference's emitted signatures) ----------- */
+
+/* Select the mechanism used by the four functions below (NULL unbinds).
+ * They take HOST pointers, run one state through the same GPU kernels on
+ * the legacy default stream and return when the result is on the host.
+ * They are serialised by a process-wide lock.  Failures leave NaN in the
+ * outputs and a message in crs_last_error(). */
+int crs_bind(const crs_mech *mech);
+
+/* rate_subs.py:1297-1299 (chem_utils.h) */
+void eval_conc(const double T, const double pres, const double *y,
+               double *y_N, double *mw_avg, double *rho, double *conc);
+/* rate_subs.py:287-290 (rates.h) */
+void eval_rxn_rates(const double T, const double pres, const double *C,
+                    double *fwd_rxn_rates, double *rev_rxn_rates);
+/* rate_subs.py:761-763 (rates.h; emitted only when N_pm > 0) */
+void get_rxn_pres_mod(const double T, const double pres, const double *C,
+                      double *pres_mod);
+/* rate_subs.py:1124-1127 (rates.h) */
+void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
+                     const double *pres_mod, double *sp_rates, double *dy_N);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CRS_H */

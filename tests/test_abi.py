@@ -1,0 +1,62 @@
+"""libcrs: it builds, loads, exports every symbol of include/crs.h and
+rejects bad input before touching a GPU (CPU only)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+from create_rate_subs_gb300 import _lib, tables
+
+
+def header_functions():
+    with open(os.path.join(REPO, "include", "crs.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text)) - {"defined"})
+
+
+def test_header_lists_the_reference_signatures():
+    fns = header_functions()
+    for name in ("eval_conc", "eval_rxn_rates", "get_rxn_pres_mod",
+                 "eval_spec_rates", "crs_wdot", "crs_mech_load"):
+        assert name in fns
+
+
+def test_library_exports_every_header_symbol():
+    lib = _lib.load()
+    missing = [f for f in header_functions() if not hasattr(lib, f)]
+    assert not missing, missing
+
+
+def test_bad_blob_rejected_without_gpu():
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.crs_mech_load(b"NOTABLOB" + b"\0" * 64, 72, ctypes.byref(h))
+    assert rc == 2
+    assert "magic" in _lib.last_error()
+    rc = lib.crs_mech_load(None, 0, ctypes.byref(h))
+    assert rc == 1
+
+
+def test_corrupt_index_rejected(golden):
+    """A species index out of range in the tables is refused at load time,
+    so no kernel can index outside its arrays."""
+    mech, _ = golden("small")
+    t = dict(mech.tables)
+    t["nu_sp"] = t["nu_sp"].copy()
+    t["nu_sp"][0] = 999
+    blob = tables.pack(t)
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.crs_mech_load(blob, len(blob), ctypes.byref(h)) == 2
+    assert "nu species" in _lib.last_error()
+
+
+def test_per_state_call_without_binding_sets_error():
+    lib = _lib.load()
+    lib.crs_bind(None)
+    out = (ctypes.c_double * 40)()
+    lib.eval_rxn_rates(1000.0, 101325.0, out, out, out)
+    assert "no mechanism bound" in _lib.last_error()

@@ -1,0 +1,193 @@
+"""GPU parity: libcrs kernels against the reference's outputs.
+
+Reference values are the golden vectors (produced by the reference's own
+emitted C) and, for fresh random states, the CPU oracle, which is pinned
+bit-exact to those vectors (tests/test_oracle.py).
+
+Tolerances
+* CRS_MODE_FP64_STRICT: concentrations and species-rate sums involve no
+  transcendental function and must be bit-identical; fwd / rev / pres_mod
+  differ from the host only through exp/log/pow last bits: per-entry
+  relative error <= 1e-13; wdot: scaled error <= 1e-12.
+* wdot errors use the gross-rate normalisation of oracle.wdot_errors:
+  |w - w_ref| / G with G_k = sum_r |nu_kr| (|fwd_r| + |rev_r|) pres_mod_r.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES
+from create_rate_subs_gb300 import _lib, synth
+from oracle.oracle import Oracle, gross_scale, wdot_errors
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+TOL_WDOT_FP64 = 1e-12
+TOL_STAGE_FP64 = 1e-13
+
+
+def _rs(mech):
+    from create_rate_subs_gb300.rates import RateSubs
+    return RateSubs(mech)
+
+
+def _dev(*arrs):
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+
+
+def _relmax(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    d = np.abs(a - b)
+    s = np.abs(b)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        r = np.where(s > 0, d / s, d)
+    return float(np.max(r)) if r.size else 0.0
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_strict_stages_vs_golden(case, golden):
+    mech, g = golden(case)
+    rs = _rs(mech)
+    T, P, Y = _dev(g["T"], g["P"], g["Y"])
+    out = {k: v.cpu().numpy() for k, v in rs.wdot_stages(T, P, Y, "fp64_strict").items()}
+    assert np.array_equal(out["conc"], g["conc"])
+    assert _relmax(out["fwd"], g["fwd"]) <= TOL_STAGE_FP64
+    assert _relmax(out["rev"], g["rev"]) <= TOL_STAGE_FP64
+    assert _relmax(out["pm"], g["pm"]) <= TOL_STAGE_FP64
+    G = gross_scale(mech.tables, g["fwd"], g["rev"], g["pm"])
+    err = wdot_errors(out["wdot"], g["wdot"], G)
+    assert err["scaled"] <= TOL_WDOT_FP64, err
+    assert rs.status() == (0, 0)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_batched_reference_functions_vs_golden(case, golden):
+    """The four reference functions, batched, stage by stage."""
+    mech, g = golden(case)
+    rs = _rs(mech)
+    T, P, Y, C, F, R, PM = _dev(g["T"], g["P"], g["Y"], g["conc"], g["fwd"],
+                                g["rev"], g["pm"])
+    y_N, mw, rho, conc = rs.eval_conc(T, P, Y)
+    assert np.array_equal(conc.cpu().numpy(), g["conc"])
+    assert np.array_equal(torch.stack([y_N, mw, rho]).cpu().numpy(), g["misc"])
+    fwd, rev = rs.eval_rxn_rates(T, P, C)
+    assert _relmax(fwd.cpu().numpy(), g["fwd"]) <= TOL_STAGE_FP64
+    assert _relmax(rev.cpu().numpy(), g["rev"]) <= TOL_STAGE_FP64
+    pm = rs.get_rxn_pres_mod(T, P, C)
+    assert _relmax(pm.cpu().numpy(), g["pm"]) <= TOL_STAGE_FP64
+    # spec rates from the reference's own fwd/rev/pm: only + and *, so exact
+    w = rs.eval_spec_rates(F, R, PM)
+    assert np.array_equal(w.cpu().numpy(), g["wdot"])
+
+
+@pytest.mark.parametrize("case", ["small", "features"])
+def test_per_state_dropin(case, golden):
+    """The reference's per-state signatures, through crs_bind."""
+    mech, g = golden(case)
+    rs = _rs(mech)
+    lib = _lib.load()
+    _lib.check(lib.crs_bind(rs.h))
+    N, R, NREV, NPM = (int(x) for x in g["dims"])
+    dp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    try:
+        for i in (0, 5, g["T"].shape[0] - 1):
+            y = np.ascontiguousarray(g["Y"][: N - 1, i])
+            conc = np.zeros(N)
+            yN, mw, rho = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double())
+            lib.eval_conc(g["T"][i], g["P"][i], dp(y), ctypes.byref(yN),
+                          ctypes.byref(mw), ctypes.byref(rho), dp(conc))
+            assert np.array_equal(conc, g["conc"][:, i])
+            assert (yN.value, mw.value, rho.value) == tuple(g["misc"][:, i])
+            C = np.ascontiguousarray(g["conc"][:, i])
+            fwd, rev, pm = np.zeros(R), np.zeros(max(NREV, 1)), np.zeros(max(NPM, 1))
+            lib.eval_rxn_rates(g["T"][i], g["P"][i], dp(C), dp(fwd), dp(rev))
+            assert _relmax(fwd, g["fwd"][:, i]) <= TOL_STAGE_FP64
+            assert _relmax(rev[:NREV], g["rev"][:, i]) <= TOL_STAGE_FP64
+            lib.get_rxn_pres_mod(g["T"][i], g["P"][i], dp(C), dp(pm))
+            assert _relmax(pm[:NPM], g["pm"][:, i]) <= TOL_STAGE_FP64
+            F = np.ascontiguousarray(g["fwd"][:, i])
+            Rr = np.ascontiguousarray(g["rev"][:, i]) if NREV else np.zeros(1)
+            PMr = np.ascontiguousarray(g["pm"][:, i]) if NPM else np.zeros(1)
+            sp = np.zeros(N)
+            dyN = ctypes.c_double()
+            lib.eval_spec_rates(dp(F), dp(Rr), dp(PMr), dp(sp), ctypes.byref(dyN))
+            assert np.array_equal(sp[: N - 1], g["wdot"][: N - 1, i])
+            assert dyN.value == g["wdot"][N - 1, i]
+    finally:
+        lib.crs_bind(None)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 127, 129, 1000])
+def test_odd_sizes_and_tails(n, synth_mech):
+    mech = synth_mech("gri53")
+    T, P, Y = synth.make_states(mech.n_species, n, seed=n)
+    ref = Oracle(mech.blob).eval(T, P, Y)
+    G = gross_scale(mech.tables, ref["fwd"], ref["rev"], ref["pm"])
+    rs = _rs(mech)
+    dT, dP, dY = _dev(T, P, Y)
+    for mode in ("fp64_strict",):
+        w = rs.wdot(dT, dP, dY, mode).cpu().numpy()
+        assert wdot_errors(w, ref["wdot"], G)["scaled"] <= TOL_WDOT_FP64
+
+
+def test_strided_soa(synth_mech):
+    """ld > n: states embedded in a wider SoA buffer."""
+    mech = synth_mech("small")
+    n, ld = 300, 512
+    T, P, Y = synth.make_states(mech.n_species, n, seed=3)
+    ref = Oracle(mech.blob).eval(T, P, Y)
+    G = gross_scale(mech.tables, ref["fwd"], ref["rev"], ref["pm"])
+    rs = _rs(mech)
+    big = np.zeros((mech.n_species, ld))
+    big[:, :n] = Y
+    dT, dP, dY = _dev(T, P, big)
+    dY = dY[:, :n]
+    w = rs.wdot(dT, dP, dY, "fp64_strict").cpu().numpy()
+    assert wdot_errors(w, ref["wdot"], G)["scaled"] <= TOL_WDOT_FP64
+
+
+def test_random_states_gri53(synth_mech):
+    mech = synth_mech("gri53")
+    n = 1 << 14
+    T, P, Y = synth.make_states(mech.n_species, n, seed=1234)
+    ref = Oracle(mech.blob).eval(T, P, Y)
+    G = gross_scale(mech.tables, ref["fwd"], ref["rev"], ref["pm"])
+    rs = _rs(mech)
+    dT, dP, dY = _dev(T, P, Y)
+    w = rs.wdot(dT, dP, dY, "fp64_strict").cpu().numpy()
+    assert wdot_errors(w, ref["wdot"], G)["scaled"] <= TOL_WDOT_FP64
+
+
+def test_nonfinite_inputs_are_counted(synth_mech):
+    """A NaN temperature yields non-finite wdot and is reported through the
+    status word, not by trapping."""
+    mech = synth_mech("small")
+    T, P, Y = synth.make_states(mech.n_species, 64, seed=5)
+    T[7] = np.nan
+    rs = _rs(mech)
+    rs.reset_status()
+    dT, dP, dY = _dev(T, P, Y)
+    w = rs.wdot(dT, dP, dY, "fp64_strict").cpu().numpy()
+    flags, bad = rs.status()
+    assert flags == 0
+    assert bad == int(np.sum(~np.isfinite(w))) and bad > 0
+    assert np.all(np.isfinite(np.delete(w, 7, axis=1)))
+
+
+def test_argument_errors(synth_mech):
+    mech = synth_mech("small")
+    rs = _rs(mech)
+    lib = _lib.load()
+    rc = lib.crs_wdot(rs.h, -1, None, None, None, 0, None, 0, None)
+    assert rc == 1
+    rc = lib.crs_wdot(rs.h, 10, None, None, None, 5, None, 0, None)
+    assert rc == 1
+    T, P, Y = _dev(*synth.make_states(mech.n_species, 8, seed=1))
+    w = torch.empty((mech.n_species, 8), dtype=torch.float64, device="cuda")
+    rc = lib.crs_wdot(rs.h, 8, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(P.data_ptr()),
+                      ctypes.c_void_p(Y.data_ptr()), 8, ctypes.c_void_p(w.data_ptr()), 99, None)
+    assert rc == 1
