@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--states", type=int, default=N_STATES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one launch of each wdot kernel on 2^18 states (for ncu)")
     return ap.parse_args()
 
 
@@ -245,7 +247,7 @@ def run_ours(args):
     peaks = dict(fp64_fma_ops=pk[0], fp64_exp=pk[1], fp32_fma_ops=pk[2], sfu_ex2=pk[3])
 
     modes = {}
-    for m in ("fp64", "fp64_strict", "mixed"):
+    for m in ("fp64", "fp64_strict", "mixed", "fp64_tps", "mixed_tps", "fp64_warp", "mixed_warp"):
         try:
             rs.wdot(dT[:1024], dP[:1024], dY[:, :1024], mode=m)
             modes[m] = True
@@ -260,6 +262,19 @@ def run_ours(args):
                      args.warmup, stream, dist)
     clocks = clk.stop()
     value = n * world / (ms * 1e-3)
+    per_mode = {}
+    for m in modes:
+        msm = _time_steps(lambda: rs.wdot(dT, dP, dY, m, out=out), max(2, args.steps // 2), 1,
+                          stream, dist)
+        per_mode[m] = {"value": n * world / (msm * 1e-3), "ms_per_step": msm}
+    strict = None
+    if plain != "fp64_strict":
+        ms_s = _time_steps(lambda: rs.wdot(dT, dP, dY, "fp64_strict", out=out),
+                           max(2, args.steps // 2), 1, stream, dist)
+        strict = {"value": n * world / (ms_s * 1e-3), "unit": "states/s",
+                  "ms_per_step": ms_s,
+                  "note": "FP64 in the reference's own operation order (CUDA exp/log/pow, "
+                          "divisions), same workload"}
 
     # accuracy of each mode against the strict FP64 kernel on a sub-sample
     sub = min(n, 1 << 15)
@@ -327,7 +342,8 @@ def run_ours(args):
         "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": _config(n), "plain_mode": plain,
+        "config": _config(n), "plain_mode": plain, "fp64_strict": strict,
+        "modes_states_per_s": per_mode,
         "accuracy_vs_fp64_strict": accuracy,
         "mixed": mixed,
         "e2e": {"value": n * world / (ms_e2e * 1e-3), "unit": "states/s",
@@ -399,8 +415,31 @@ def _scaled_error(tables, w, ref):
                                  "rel over |w64|>=1e-3 G"}
 
 
+def run_profile(args):
+    """One launch per mode on 2^18 states: the case the ncu summaries in
+    profiles/ were captured on."""
+    import torch
+    from create_rate_subs_gb300 import synth
+    from create_rate_subs_gb300.rates import RateSubs
+    torch.cuda.set_device(0)
+    mech = _mechanism()
+    rs = RateSubs(mech)
+    n = 1 << 18
+    T, P, Y = synth.make_states(mech.n_species, n, seed=5)
+    dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[:-1].copy()))
+    out = torch.empty((mech.n_species, n), dtype=torch.float64, device="cuda")
+    for mode in ("fp64_strict", "fp64", "mixed", "fp64_tps", "mixed_tps", "fp64_warp", "mixed_warp"):
+        rs.wdot(dT, dP, dY, mode, out=out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "gri53, %d states, one launch per mode" % n,
+                      "status": rs.status()}))
+    return 0
+
+
 def main():
     args = _args()
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -18,7 +18,8 @@ CRS_OK = 0
 ERRORS = {1: "bad argument", 2: "bad mechanism tables", 3: "CUDA error",
           4: "unsupported", 5: "timeout", 6: "no mechanism bound"}
 
-MODES = {"fp64": 0, "fp64_strict": 1, "mixed": 2}
+MODES = {"fp64": 0, "fp64_strict": 1, "mixed": 2, "fp64_tps": 3, "mixed_tps": 4,
+         "fp64_warp": 5, "mixed_warp": 6}
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -35,6 +36,7 @@ def _sig(lib):
     s = {
         "crs_mech_load": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
         "crs_mech_load_file": [ctypes.c_char_p, ctypes.POINTER(_vp)],
+        "crs_mech_inspect": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_i64)],
         "crs_mech_free": [_vp],
         "crs_mech_dims": [_vp, ctypes.POINTER(_i64)],
         "crs_status": [_vp, _vp, ctypes.POINTER(ctypes.c_int32)],

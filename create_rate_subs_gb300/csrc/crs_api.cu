@@ -23,13 +23,18 @@ cudaError_t launch_wdot_fp64(const unsigned char *img, const ImgLayout &L,
 cudaError_t launch_wdot_mixed(const unsigned char *img, const ImgLayout &L,
                               const Batch &b, int sm_count, int smem_optin,
                               cudaStream_t s);
+cudaError_t launch_wdot_fp64_tps(const unsigned char *img, const ImgLayout &L,
+                                 const Batch &b, int sm_count, int smem_optin,
+                                 cudaStream_t s);
+cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
+                                  const Batch &b, int sm_count, int smem_optin,
+                                  cudaStream_t s);
 cudaError_t launch_stage(int which, const unsigned char *img,
                          const ImgLayout &L, const Batch &b, double *y_N,
                          double *mw, double *rho, int sm_count, cudaStream_t s);
-// Derived tables appended to the image by the fast kernels' builders.
-bool build_fast_tables(const std::vector<unsigned char> &blob_img,
-                       const ImgLayout &L, std::vector<unsigned char> &extra,
-                       int base_offset, ImgLayout &out);
+// Tables the fast kernels derive from the blob's tables at load time.
+bool build_fast_tables(const std::vector<unsigned char> &img,
+                       const ImgLayout &L, std::vector<Derived> &extra);
 }  // namespace crs
 
 struct crs_mech {
@@ -112,15 +117,16 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   L.NRATE = (int)dims[4];
   if (L.N < 2 || L.R < 0 || L.NREV < 0 || L.NPM < 0 || L.NRATE < L.R)
     return fail(CRS_ERR_BLOB, "bad dims");
+  // Sections the fast kernels read come first; the ones only the
+  // reference-order kernels read (per-reaction Kc polynomials, raw NASA-7
+  // coefficients) come last, so that fast kernels stage a prefix.
   Want want[] = {
       {"sp_inv_mw", &L.inv_mw, 1}, {"rate_par", &L.rate_par, 1},
       {"rx_nu", &L.rx_nu, 1}, {"px_nu", &L.px_nu, 1},
-      {"kc_tmid", &L.kc_tmid, 1}, {"kc_lo", &L.kc_lo, 1},
-      {"kc_hi", &L.kc_hi, 1}, {"kc_pref", &L.kc_pref, 1},
+      {"kc_pref", &L.kc_pref, 1},
       {"pm_eff_val", &L.pm_eff_val, 1}, {"pm_troe", &L.pm_troe, 1},
       {"pm_sri", &L.pm_sri, 1}, {"nu_val", &L.nu_val, 1},
-      {"sp_tmid", &L.sp_tmid, 1}, {"sp_lo", &L.sp_lo, 1},
-      {"sp_hi", &L.sp_hi, 1}, {"kc_dnu", &L.kc_dnu, 1},
+      {"sp_tmid", &L.sp_tmid, 1}, {"kc_dnu", &L.kc_dnu, 1},
       {"rate_kind", &L.rate_kind, 2}, {"rate_npow", &L.rate_npow, 2},
       {"rx_ptr", &L.rx_ptr, 2}, {"rx_sp", &L.rx_sp, 2},
       {"rx_nint", &L.rx_nint, 2}, {"px_ptr", &L.px_ptr, 2},
@@ -132,6 +138,10 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       {"pm_k0", &L.pm_k0, 2}, {"pm_kinf", &L.pm_kinf, 2},
       {"pm_troe_t2", &L.pm_troe_t2, 2}, {"pm_sri_de", &L.pm_sri_de, 2},
       {"nu_ptr", &L.nu_ptr, 2}, {"nu_sp", &L.nu_sp, 2},
+      // reference-order only
+      {"kc_tmid", &L.kc_tmid, 1}, {"kc_lo", &L.kc_lo, 1},
+      {"kc_hi", &L.kc_hi, 1}, {"sp_lo", &L.sp_lo, 1},
+      {"sp_hi", &L.sp_hi, 1},
   };
   std::vector<unsigned char> &img = m->h_img;
   img.clear();
@@ -199,15 +209,101 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
         (!in(t.pm_k0[p], 0, L.NRATE) || !in(t.pm_kinf[p], 0, L.NRATE)))
       return fail(CRS_ERR_BLOB, "bad fall-off rate rows");
   }
-  // Derived tables of the fast kernels.
-  std::vector<unsigned char> extra;
-  crs::ImgLayout L2 = L;
-  if (!crs::build_fast_tables(img, L, extra, (int)img.size(), L2))
+  // Final image: sections in the order the kernels stage them.  [F] is
+  // read only by the FP64 kernel, [S] by both fast kernels, [M] only by the
+  // mixed kernel; all of them are per-reaction tables that go to shared
+  // memory.  The rest (fall-off constants, raw NASA-7 data, per-reaction Kc
+  // polynomials of the reference-order kernel) stays in global memory.
+  std::vector<crs::Derived> derived;
+  if (!crs::build_fast_tables(img, L, derived))
     return fail(CRS_ERR_BLOB, "could not derive fast tables");
-  img.insert(img.end(), extra.begin(), extra.end());
-  img.resize((img.size() + 15) / 16 * 16);
+  using M = int crs::ImgLayout::*;
+  std::vector<std::pair<M, std::vector<unsigned char>>> secs;
+  auto raw = [&](M f, const char *name) {
+    const int64_t c = cnt(name);
+    size_t es = 8;
+    for (auto &w : want)
+      if (strcmp(w.name, name) == 0) es = w.dtype == 1 ? 8 : 4;
+    const unsigned char *src = img.data() + (L.*f);
+    secs.emplace_back(f, std::vector<unsigned char>(src, src + c * es));
+  };
+  auto der = [&](M f) {
+    for (auto &d : derived)
+      if (d.field == f) secs.emplace_back(f, d.bytes);
+  };
+  using IL = crs::ImgLayout;
+  // Region order T F S M D (see ImgLayout::rng):
+  // [T] one-state-per-thread tables
+  der(&IL::perm); der(&IL::seg); der(&IL::rfac); der(&IL::pfac);
+  const size_t iF = secs.size();
+  // [F] FP64 only
+  der(&IL::exptab); der(&IL::rate_x);
+  const size_t iS = secs.size();
+  // [S] shared by the fast kernels
+  der(&IL::kc_lpref); der(&IL::sp_gibbs);
+  raw(&IL::sp_tmid, "sp_tmid"); raw(&IL::inv_mw, "sp_inv_mw");
+  raw(&IL::rate_kind, "rate_kind"); raw(&IL::rx_ptr, "rx_ptr");
+  raw(&IL::rx_sp, "rx_sp"); raw(&IL::rx_nint, "rx_nint");
+  raw(&IL::px_ptr, "px_ptr"); raw(&IL::px_sp, "px_sp");
+  raw(&IL::px_nint, "px_nint"); raw(&IL::rev_idx, "rev_idx");
+  raw(&IL::pm_idx, "pm_idx"); raw(&IL::nu_ptr, "nu_ptr");
+  raw(&IL::nu_sp, "nu_sp"); raw(&IL::nu_val, "nu_val");
+  const size_t iM = secs.size();
+  // [M] mixed only
+  der(&IL::rate_ff); der(&IL::inv_mw_f);
+  const size_t iD = secs.size();
+  // [D] one-state-per-warp tables
+  der(&IL::dperm); der(&IL::spc_ptr); der(&IL::spc_r); der(&IL::spc_nu);
+  der(&IL::lane_ptr); der(&IL::lane_sp);
+  const size_t iC = secs.size();
+  // cold: read from global memory
+  raw(&IL::rate_npow, "rate_npow"); raw(&IL::rx_nu, "rx_nu");
+  raw(&IL::px_nu, "px_nu"); raw(&IL::pm_eff_val, "pm_eff_val");
+  raw(&IL::pm_kind, "pm_kind"); raw(&IL::pm_form, "pm_form");
+  raw(&IL::pm_sp, "pm_sp"); raw(&IL::pm_eff_ptr, "pm_eff_ptr");
+  raw(&IL::pm_eff_sp, "pm_eff_sp"); raw(&IL::pm_k0, "pm_k0");
+  raw(&IL::pm_kinf, "pm_kinf"); raw(&IL::pm_troe_t2, "pm_troe_t2");
+  raw(&IL::pm_sri_de, "pm_sri_de");
+  der(&IL::troe_x); der(&IL::sri_x); der(&IL::troe_ff); der(&IL::sri_ff);
+  der(&IL::eff_f);
+  raw(&IL::rate_par, "rate_par"); raw(&IL::kc_pref, "kc_pref");
+  raw(&IL::pm_troe, "pm_troe"); raw(&IL::pm_sri, "pm_sri");
+  raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::kc_ptr, "kc_ptr");
+  raw(&IL::kc_tmid, "kc_tmid"); raw(&IL::kc_lo, "kc_lo");
+  raw(&IL::kc_hi, "kc_hi"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
+  // every blob section and every derived table must have been placed
+  for (auto &w : want) {
+    bool found = false;
+    for (auto &sec : secs) found |= (sec.first == (M)nullptr) ? false : (&(L.*(sec.first)) == w.field);
+    if (!found) return fail(CRS_ERR_BLOB, "internal: section %s not placed", w.name);
+  }
+  for (auto &d : derived) {
+    bool found = false;
+    for (auto &sec : secs) found |= sec.first == d.field;
+    if (!found) return fail(CRS_ERR_BLOB, "internal: derived table not placed");
+  }
+  std::vector<unsigned char> out;
+  crs::ImgLayout L2 = L;
+  std::vector<int> starts;
+  for (auto &sec : secs) {
+    const size_t off = (out.size() + 15) / 16 * 16;
+    out.resize(off + sec.second.size() + 16);  // +16 keeps empty sections valid
+    if (!sec.second.empty()) memcpy(out.data() + off, sec.second.data(), sec.second.size());
+    L2.*(sec.first) = (int)off;
+    starts.push_back((int)off);
+  }
+  out.resize((out.size() + 15) / 16 * 16);
+  L2.bytes = (int)out.size();
+  starts.push_back((int)out.size());
+  const int T0 = starts[0], F0 = starts[iF], S0 = starts[iS], M0 = starts[iM],
+            D0 = starts[iD], C0 = starts[iC];
+  const int rng[4][4] = {{T0, M0, 0, 0},    // FP64 per thread: T F S
+                         {F0, M0, D0, C0},  // FP64 per warp: F S + D
+                         {T0, F0, S0, D0},  // mixed per thread: T + S M
+                         {S0, C0, 0, 0}};   // mixed per warp: S M D
+  memcpy(L2.rng, rng, sizeof rng);
+  img.swap(out);
   L = L2;
-  L.bytes = (int)img.size();
   return CRS_OK;
 }
 
@@ -271,6 +367,25 @@ int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
   // reserve the static __shared__ mbarrier and a little slack
   m->smem_optin -= 64;
   *out = m;
+  return CRS_OK;
+}
+
+int crs_mech_inspect(const void *blob, size_t nbytes, int64_t out[6]) {
+  if (!blob || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  crs_mech m;
+  int rc = build_image(static_cast<const unsigned char *>(blob), nbytes, &m);
+  if (rc != CRS_OK) return rc;
+  const int64_t block = 128, N = m.L.N;
+  out[0] = m.L.bytes;
+  auto span = [&](int r) {
+    return (int64_t)(m.L.rng[r][1] - m.L.rng[r][0] + m.L.rng[r][3] - m.L.rng[r][2]);
+  };
+  const int64_t R = m.L.R;
+  out[1] = span(1);
+  out[2] = span(3);
+  out[3] = span(1) + 8 * 8 * (128 + 2 * N + R + 1);          // CRS_MODE_FP64 per CTA
+  out[4] = span(3) + 8 * 8 * (128 + N + R + (N + 1) / 2 + 1);  // CRS_MODE_MIXED per CTA
+  out[5] = out[0] + 2 * N * block * 8;   // CRS_MODE_FP64_STRICT, all on chip
   return CRS_OK;
 }
 
@@ -395,9 +510,26 @@ int crs_wdot_stages(const crs_mech *m, int64_t n, const double *T,
       e = crs::launch_wdot_strict(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_FP64:
-      e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      // one state per thread when its columns fit on chip, else per warp
+      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      if (e == cudaErrorNotSupported)
+        e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_MIXED:
+      e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      if (e == cudaErrorNotSupported)
+        e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64_TPS:
+      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED_TPS:
+      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64_WARP:
+      e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED_WARP:
       e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     default:

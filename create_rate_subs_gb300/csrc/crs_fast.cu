@@ -1,27 +1,752 @@
-// Placeholder launchers for the fast FP64 and mixed-precision kernels.
+// CRS_MODE_FP64: FP64 throughout, restructured for GB300's FP64 pipe.
+//
+// On this part an FP64 instruction costs ~70 FP32 instructions, so the
+// kernel is bound by the number of FP64 instructions per state.  Compared
+// with the reference's operation order (crs_fp64_strict.cu) it
+//  * evaluates exp with a table-driven method (Tang, ACM TOMS 15(2), 1989:
+//    x = (256 k + j) ln2/256 + r, exp(x) = 2^k 2^(j/256) p(r), |r| <=
+//    ln2/512, p the degree-4 Taylor polynomial; error below 1 ulp plus the
+//    table rounding) -- 9 FP64 instructions instead of ~19 for CUDA's exp;
+//  * multiplies by 1/T (one division per state) instead of dividing;
+//  * forms the equilibrium constant from per-species Gibbs terms
+//    S_k = s_k/R - h_k/RT - ln T evaluated once per state (the reference
+//    sums the same NASA-7 coefficients per reaction on the host), and folds
+//    1/Kc into the reverse rate constant: kr = exp(x_f - sum nu S - ln p),
+//    one exponential instead of exp + exp + divide;
+//  * computes the fall-off reduced pressure as exp(x_0 - x_inf) * [M].
+// Results stay within 1e-12 (gross-rate scaled) of the reference.
 #include <cuda_runtime.h>
+#include <math.h>
 
+#include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "crs_internal.cuh"
+#include "crs_shapes.cuh"
 
 namespace crs {
 
-bool build_fast_tables(const std::vector<unsigned char> &, const ImgLayout &L,
-                       std::vector<unsigned char> &extra, int, ImgLayout &out) {
+// ---- derived tables (host) ----------------------------------------------
+namespace {
+template <class T>
+void put(std::vector<Derived> &v, int ImgLayout::*field, const std::vector<T> &src) {
+  Derived d;
+  d.field = field;
+  d.bytes.resize(src.size() * sizeof(T));
+  if (!src.empty()) memcpy(d.bytes.data(), src.data(), d.bytes.size());
+  v.push_back(std::move(d));
+}
+}  // namespace
+
+bool build_fast_tables(const std::vector<unsigned char> &img,
+                       const ImgLayout &L, std::vector<Derived> &extra) {
+  const Tab t = make_tab(img.data(), L);
   extra.clear();
-  out = L;
+  // per rate row: logA, b, -Ta (EXP kind); A, b, -Ta (other kinds)
+  std::vector<double> rx(3 * (size_t)L.NRATE);
+  for (int r = 0; r < L.NRATE; ++r) {
+    const double *p = t.rate_par + 4 * r;
+    rx[3 * r + 0] = (t.rate_kind[r] == RATE_EXP) ? p[1] : p[0];
+    rx[3 * r + 1] = p[2];
+    rx[3 * r + 2] = -p[3];
+  }
+  std::vector<double> lp(L.NREV > 0 ? L.NREV : 1);
+  for (int j = 0; j < L.NREV; ++j) lp[j] = std::log(t.kc_pref[j]);
+  std::vector<double> tx(5 * (size_t)(L.NPM > 0 ? L.NPM : 1), 0.0);
+  std::vector<double> sx(5 * (size_t)(L.NPM > 0 ? L.NPM : 1), 0.0);
+  for (int p = 0; p < L.NPM; ++p) {
+    const double *c = t.pm_troe + 5 * p;
+    tx[5 * p + 0] = c[0];
+    tx[5 * p + 1] = -1.0 / c[1];
+    tx[5 * p + 2] = c[2];
+    tx[5 * p + 3] = -1.0 / c[3];
+    tx[5 * p + 4] = -c[4];
+    const double *s = t.pm_sri + 5 * p;
+    sx[5 * p + 0] = s[0];
+    sx[5 * p + 1] = -s[1];
+    sx[5 * p + 2] = -1.0 / s[2];
+    sx[5 * p + 3] = s[3];
+    sx[5 * p + 4] = s[4];
+  }
+  // S_k(T) = g0 + g1 ln T + T (g2 + T (g3 + T (g4 + g5 T))) + g6 / T
+  std::vector<double> g(14 * (size_t)L.N);
+  for (int k = 0; k < L.N; ++k) {
+    for (int h = 0; h < 2; ++h) {
+      const double *a = (h ? t.sp_hi : t.sp_lo) + 7 * k;
+      double *o = g.data() + 14 * k + 7 * h;
+      o[0] = a[6] - a[0];
+      o[1] = a[0] - 1.0;
+      o[2] = a[1] / 2.0;
+      o[3] = a[2] / 6.0;
+      o[4] = a[3] / 12.0;
+      o[5] = a[4] / 20.0;
+      o[6] = -a[5];
+    }
+  }
+  std::vector<double> et(256);
+  for (int j = 0; j < 256; ++j) et[j] = (double)exp2l((long double)j / 256.0L);
+  put(extra, &ImgLayout::rate_x, rx);
+  put(extra, &ImgLayout::kc_lpref, lp);
+  put(extra, &ImgLayout::troe_x, tx);
+  put(extra, &ImgLayout::sri_x, sx);
+  put(extra, &ImgLayout::sp_gibbs, g);
+  put(extra, &ImgLayout::exptab, et);
+  // mixed-precision tables
+  auto split = [](double v, float *h, float *l) {
+    *h = (float)v;
+    *l = (float)(v - (double)*h);
+  };
+  std::vector<float> rf(8 * (size_t)L.NRATE, 0.0f);
+  for (int r = 0; r < L.NRATE; ++r) {
+    const double *p = t.rate_par + 4 * r;  // A, logA, b, Ta
+    double lnA = std::log(std::fabs(p[0]));
+    double bb = p[2];
+    if (t.rate_kind[r] == RATE_POW) bb = (double)t.rate_npow[r];
+    if (t.rate_kind[r] == RATE_CONST) bb = 0.0;
+    const double nTa = (t.rate_kind[r] == RATE_POW || t.rate_kind[r] == RATE_CONST) ? 0.0 : -p[3];
+    split(lnA, &rf[8 * r + 0], &rf[8 * r + 1]);
+    split(bb, &rf[8 * r + 2], &rf[8 * r + 3]);
+    split(nTa, &rf[8 * r + 4], &rf[8 * r + 5]);
+    rf[8 * r + 6] = p[0] < 0 ? -1.0f : 1.0f;
+  }
+  std::vector<float> imf(L.N);
+  for (int k = 0; k < L.N; ++k) imf[k] = (float)t.inv_mw[k];
+  std::vector<float> tf(8 * (size_t)(L.NPM > 0 ? L.NPM : 1), 0.0f);
+  std::vector<float> sf(8 * (size_t)(L.NPM > 0 ? L.NPM : 1), 0.0f);
+  for (int p = 0; p < L.NPM; ++p) {
+    const double *c = tx.data() + 5 * p;  // P0, -1/T3, P2, -1/T1, -T2
+    tf[8 * p + 0] = (float)c[0];
+    split(c[1], &tf[8 * p + 1], &tf[8 * p + 2]);
+    tf[8 * p + 3] = (float)c[2];
+    split(c[3], &tf[8 * p + 4], &tf[8 * p + 5]);
+    split(c[4], &tf[8 * p + 6], &tf[8 * p + 7]);
+    const double *d = sx.data() + 5 * p;  // a, -b, -1/c, d, e
+    sf[8 * p + 0] = (float)d[0];
+    split(d[1], &sf[8 * p + 1], &sf[8 * p + 2]);
+    split(d[2], &sf[8 * p + 3], &sf[8 * p + 4]);
+    sf[8 * p + 5] = (float)d[3];
+    sf[8 * p + 6] = (float)d[4];
+  }
+  const int ne = t.pm_eff_ptr[L.NPM];
+  std::vector<float> ef(ne > 0 ? ne : 1, 0.0f);
+  for (int e = 0; e < ne; ++e) ef[e] = (float)t.pm_eff_val[e];
+  put(extra, &ImgLayout::rate_ff, rf);
+  put(extra, &ImgLayout::inv_mw_f, imf);
+  put(extra, &ImgLayout::troe_ff, tf);
+  put(extra, &ImgLayout::sri_ff, sf);
+  put(extra, &ImgLayout::eff_f, ef);
+  // reaction order for the shape-specialised paths and expanded factors
+  std::vector<int32_t> rfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0),
+      pfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0), shape(L.R, NSHAPE);
+  for (int r = 0; r < L.R; ++r) {
+    bool ok = t.rate_kind[r] == RATE_EXP && t.pm_idx[r] < 0;
+    int nr = 0, np = 0;
+    for (int q = t.rx_ptr[r]; q < t.rx_ptr[r + 1]; ++q) {
+      if (t.rx_nint[q] < 0) ok = false;
+      for (int c = 0; c < t.rx_nint[q] && ok; ++c) {
+        if (nr < MAXF) rfac[(size_t)MAXF * r + nr] = t.rx_sp[q];
+        ++nr;
+      }
+    }
+    for (int q = t.px_ptr[r]; q < t.px_ptr[r + 1]; ++q) {
+      if (t.px_nint[q] < 0) ok = false;
+      for (int c = 0; c < t.px_nint[q] && ok; ++c) {
+        if (np < MAXF) pfac[(size_t)MAXF * r + np] = t.px_sp[q];
+        ++np;
+      }
+    }
+    const int nnu = t.nu_ptr[r + 1] - t.nu_ptr[r];
+    const int rev = t.rev_idx[r] >= 0;
+    if (!ok) continue;
+    for (int sh = 0; sh < NSHAPE; ++sh) {
+      const Shape d = shape_of(sh);
+      if (d.nr == nr && d.np == np && d.nnu == nnu && d.rev == rev) {
+        shape[r] = sh;
+        break;
+      }
+    }
+  }
+  std::vector<int32_t> perm, seg(NSHAPE + 1);
+  for (int sh = 0; sh <= NSHAPE; ++sh) {
+    seg[sh] = (int32_t)perm.size();
+    for (int r = 0; r < L.R; ++r)
+      if (shape[r] == sh) perm.push_back(r);
+  }
+  if (perm.empty()) perm.push_back(0);
+  put(extra, &ImgLayout::perm, perm);
+  // warp-per-state kernels: reactions ordered so that 32 consecutive ones
+  // mostly take the same code path (rate form, pressure modification,
+  // broadening, reversibility, factor counts)
+  std::vector<int32_t> dperm(L.R > 0 ? L.R : 1);
+  {
+    std::vector<std::pair<long long, int>> key;
+    for (int r = 0; r < L.R; ++r) {
+      const int p = t.pm_idx[r];
+      const long long pmk = p < 0 ? 0 : 1 + t.pm_kind[p] * 3 + t.pm_form[p];
+      const long long nr = t.rx_ptr[r + 1] - t.rx_ptr[r];
+      const long long np = t.px_ptr[r + 1] - t.px_ptr[r];
+      const long long k = ((((long long)(t.rate_kind[r] != RATE_EXP) * 16 + pmk) * 2 +
+                            (t.rev_idx[r] >= 0)) * 8 + nr) * 8 + np;
+      key.emplace_back(k, r);
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<long long, int> &a,
+                        const std::pair<long long, int> &b) { return a.first < b.first; });
+    for (int r = 0; r < L.R; ++r) dperm[r] = key[r].second;
+  }
+  // species-major net-nu CSR, entries in reaction order (the order in which
+  // the reference adds the terms of each species)
+  const int nnz = t.nu_ptr[L.R];
+  std::vector<int32_t> sptr(L.N + 1, 0), sr(nnz > 0 ? nnz : 1), cnt(L.N, 0);
+  std::vector<double> snu(nnz > 0 ? nnz : 1);
+  for (int e = 0; e < nnz; ++e) sptr[t.nu_sp[e] + 1]++;
+  for (int k = 0; k < L.N; ++k) sptr[k + 1] += sptr[k];
+  for (int r = 0; r < L.R; ++r)
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+      const int k = t.nu_sp[e];
+      const int at = sptr[k] + cnt[k]++;
+      sr[at] = r;
+      snu[at] = t.nu_val[e];
+    }
+  // species to lanes, balancing the number of terms per lane (longest
+  // first onto the least loaded lane)
+  std::vector<int> order(L.N);
+  for (int k = 0; k < L.N; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return sptr[a + 1] - sptr[a] > sptr[b + 1] - sptr[b];
+  });
+  std::vector<std::vector<int>> bins(32);
+  std::vector<long long> load(32, 0);
+  for (int k : order) {
+    int best = 0;
+    for (int l = 1; l < 32; ++l)
+      if (load[l] < load[best]) best = l;
+    bins[best].push_back(k);
+    load[best] += 1 + (sptr[k + 1] - sptr[k]);
+  }
+  std::vector<int32_t> lptr(33, 0), lsp;
+  for (int l = 0; l < 32; ++l) {
+    for (int k : bins[l]) lsp.push_back(k);
+    lptr[l + 1] = (int32_t)lsp.size();
+  }
+  put(extra, &ImgLayout::dperm, dperm);
+  put(extra, &ImgLayout::spc_ptr, sptr);
+  put(extra, &ImgLayout::spc_r, sr);
+  put(extra, &ImgLayout::spc_nu, snu);
+  put(extra, &ImgLayout::lane_ptr, lptr);
+  put(extra, &ImgLayout::lane_sp, lsp);
+  put(extra, &ImgLayout::seg, seg);
+  put(extra, &ImgLayout::rfac, rfac);
+  put(extra, &ImgLayout::pfac, pfac);
   return true;
 }
 
-cudaError_t launch_wdot_fp64(const unsigned char *, const ImgLayout &,
-                             const Batch &, int, int, cudaStream_t) {
-  return cudaErrorNotSupported;
+namespace fast {
+
+constexpr double INV_L = 369.3299304675746;     // 256 / ln 2
+constexpr double L_HI = 0x1.62e42fefa0000p-9;   // ln2/256, 35 bits
+constexpr double L_LO = 0x1.cf79abc9e3b3ap-48;  // ln2/256 - L_HI
+constexpr double SHIFT = 6755399441055744.0;    // 1.5 * 2^52
+constexpr double INV_RU = 0.0001202723625380408;
+constexpr double LN10 = 2.302585092994046;
+constexpr double INV_LN10 = 0.4342944819032518;
+
+// exp(x) from a 2^(j/256) table (see file comment), without the range
+// check: arguments beyond +-700 and NaN give garbage here and are replaced
+// by exp_fix.  The table index stays in [0, 255] for any input.
+__device__ __forceinline__ double exp_core(double x, const double *tab) {
+  const double t = fma(x, INV_L, SHIFT);
+  const double kd = t - SHIFT;
+  const int k = __double2loint(t);
+  double r = fma(kd, -L_HI, x);
+  r = fma(kd, -L_LO, r);
+  const double q = fma(fma(r, 1.0 / 24.0, 1.0 / 6.0), r, 0.5);
+  const double p = fma(q, r * r, r);
+  const double tj = tab[k & 255];
+  const int m = k >> 8;  // arithmetic shift: floor(k / 256)
+  const double s = __hiloint2double(__double2hiint(tj) + m * (1 << 20),
+                                    __double2loint(tj));
+  return fma(s, p, s);
+}
+// Overflow, underflow and NaN go to CUDA's exp.
+__device__ __forceinline__ double exp_fix(double x, double e) {
+  return (fabs(x) <= 700.0) ? e : exp(x);
+}
+__device__ __forceinline__ double exp_t(double x, const double *tab) {
+  return exp_fix(x, exp_core(x, tab));
 }
 
-cudaError_t launch_wdot_mixed(const unsigned char *, const ImgLayout &,
-                              const Batch &, int, int, cudaStream_t) {
-  return cudaErrorNotSupported;
+struct Col {
+  double *p;
+  int64_t stride;
+  __device__ double &operator[](int k) const { return p[(int64_t)k * stride]; }
+};
+
+// Contiguous per-warp array (warp-per-state kernels).
+struct Arr {
+  double *p;
+  __device__ double &operator[](int k) const { return p[k]; }
+};
+
+struct State {
+  double T, invT, logT;
+  const double *tab;
+};
+
+// Rate constant of row `row`; *x receives its exponent for the EXP kind.
+__device__ __forceinline__ double rate(const Tab &t, int row, const State &s,
+                                       double &x) {
+  const double *c = t.rate_x + 3 * row;  // (logA | A), b, -Ta
+  switch (t.rate_kind[row]) {
+    case RATE_EXP:
+      x = fma(c[2], s.invT, fma(c[1], s.logT, c[0]));
+      return exp_t(x, s.tab);
+    case RATE_CONST:
+      return c[0];
+    case RATE_NEGEXP:
+      return c[0] * exp_t(fma(c[2], s.invT, c[1] * s.logT), s.tab);
+    default: {
+      double k = c[0];
+      for (int j = 0; j < t.rate_npow[row]; ++j) k *= s.T;
+      return k;
+    }
+  }
+}
+
+template <class CS>
+__device__ __forceinline__ double product(const int32_t *sp, const int32_t *nint,
+                                          const double *nu, int a, int b,
+                                          const CS &C) {
+  double p = 1.0;
+  for (int j = a; j < b; ++j) {
+    const double c = C[sp[j]];
+    const int n = nint[j];
+    if (n == 1) p *= c;
+    else if (n == 2) p *= c * c;
+    else if (n >= 0) for (int q = 0; q < n; ++q) p *= c;
+    else p *= pow(c, nu[j]);
+  }
+  return p;
+}
+
+template <class CS>
+__device__ double pres_mod(const Tab &t, int p, const State &s, double mix,
+                           const CS &C) {
+  double thd = mix;
+  const int sp = t.pm_sp[p];
+  if (t.pm_kind[p] == PM_THD || sp < 0) {
+    for (int e = t.pm_eff_ptr[p]; e < t.pm_eff_ptr[p + 1]; ++e)
+      thd = fma(t.pm_eff_val[e], C[t.pm_eff_sp[e]], thd);
+    if (t.pm_kind[p] == PM_THD) return thd;
+  } else {
+    thd = C[sp];
+  }
+  const int r0 = t.pm_k0[p], ri = t.pm_kinf[p];
+  double Pr;
+  if (t.rate_kind[r0] == RATE_EXP && t.rate_kind[ri] == RATE_EXP) {
+    const double *a = t.rate_x + 3 * r0, *b = t.rate_x + 3 * ri;
+    const double x0 = fma(a[2], s.invT, fma(a[1], s.logT, a[0]));
+    const double xi = fma(b[2], s.invT, fma(b[1], s.logT, b[0]));
+    Pr = exp_t(x0 - xi, s.tab) * thd;
+  } else {
+    double x;
+    const double k0 = rate(t, r0, s, x);
+    const double ki = rate(t, ri, s, x);
+    Pr = k0 * thd / ki;
+  }
+  const bool low = t.pm_kind[p] == PM_FALL_LOW;
+  const double inv1p = 1.0 / (1.0 + Pr);
+  const int form = t.pm_form[p];
+  if (form == FORM_LINDEMANN) return low ? Pr * inv1p : inv1p;
+  const double lP = log(fmax(Pr, 1.0e-300)) * INV_LN10;
+  double F;
+  if (form == FORM_TROE) {
+    const double *c = t.troe_x + 5 * p;  // P0, -1/T3, P2, -1/T1, -T2
+    double f = c[0] * exp_t(s.T * c[1], s.tab) + c[2] * exp_t(s.T * c[3], s.tab);
+    if (t.pm_troe_t2[p]) f += exp_t(c[4] * s.invT, s.tab);
+    const double lF = log(fmax(f, 1.0e-300)) * INV_LN10;
+    const double A = lP - 0.67 * lF - 0.4;
+    const double B = 0.806 - 1.1762 * lF - 0.14 * lP;
+    F = exp_t(LN10 * lF / (1.0 + A * A / (B * B)), s.tab);
+  } else {
+    const double *c = t.sri_x + 5 * p;  // a, -b, -1/c, d, e
+    const double X = 1.0 / (1.0 + lP * lP);
+    const double base = c[0] * exp_t(c[1] * s.invT, s.tab) + exp_t(s.T * c[2], s.tab);
+    F = exp_t(X * log(base), s.tab);
+    if (t.pm_sri_de[p]) F *= c[3] * exp_t(c[4] * s.logT, s.tab);
+  }
+  return low ? F * Pr * inv1p : F * inv1p;
+}
+
+// Four reactions of one shape (crs_shapes.cuh): rate constants, products
+// and net rates with compile-time trip counts, so that the four dependency
+// chains interleave; then their wdot contributions in order.
+template <int NR, int NP, int NNU, int REV, bool STAGES>
+__device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
+                                            int cnt, const State &s,
+                                            const Col &C, const Col &S,
+                                            const Col &W, const Batch &b,
+                                            int64_t i) {
+  double net[4], x[4], e[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const double *c = t.rate_x + 3 * rr[u];
+    x[u] = fma(c[2], s.invT, fma(c[1], s.logT, c[0]));
+    e[u] = exp_core(x[u], s.tab);
+  }
+  double fwd[4], rev[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int r = rr[u];
+    double f = exp_fix(x[u], e[u]);
+#pragma unroll
+    for (int q = 0; q < NR; ++q) f *= C[t.rfac[MAXF * r + q]];
+    fwd[u] = f;
+    rev[u] = 0.0;
+    if (REV) {
+      const int e0 = t.nu_ptr[r];
+      double g = t.kc_lpref[t.rev_idx[r]];
+#pragma unroll
+      for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], S[t.nu_sp[e0 + q]], g);
+      x[u] = x[u] - g;
+      e[u] = exp_core(x[u], s.tab);
+    }
+  }
+  if (REV) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = rr[u];
+      double v = exp_fix(x[u], e[u]);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) v *= C[t.pfac[MAXF * r + q]];
+      rev[u] = v;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) net[u] = fwd[u] - rev[u];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (u >= cnt) break;
+    const int r = rr[u];
+    if (STAGES) {
+      if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd[u];
+      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[r] * b.ld + i] = rev[u];
+    }
+    const int e0 = t.nu_ptr[r];
+#pragma unroll
+    for (int q = 0; q < NNU; ++q) {
+      const int k = t.nu_sp[e0 + q];
+      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);
+    }
+  }
+}
+
+template <int SH, bool STAGES>
+__device__ __forceinline__ void run_shape(const Tab &t, const State &s,
+                                          const Col &C, const Col &S,
+                                          const Col &W, const Batch &b,
+                                          int64_t i) {
+  constexpr Shape d = shape_of(SH);
+  const int p0 = t.seg[SH], p1 = t.seg[SH + 1];
+  for (int p = p0; p < p1; p += 4) {
+    const int cnt = p1 - p < 4 ? p1 - p : 4;
+    int rr[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) rr[u] = t.perm[p + (u < cnt ? u : cnt - 1)];
+    shape_block<d.nr, d.np, d.nnu, d.rev, STAGES>(t, rr, cnt, s, C, S, W, b, i);
+  }
+}
+
+template <int SH, bool STAGES>
+struct Shapes {
+  __device__ __forceinline__ static void run(const Tab &t, const State &s,
+                                             const Col &C, const Col &S,
+                                             const Col &W, const Batch &b,
+                                             int64_t i) {
+    run_shape<SH, STAGES>(t, s, C, S, W, b, i);
+    Shapes<SH + 1, STAGES>::run(t, s, C, S, W, b, i);
+  }
+};
+template <bool STAGES>
+struct Shapes<NSHAPE, STAGES> {
+  __device__ __forceinline__ static void run(const Tab &, const State &,
+                                             const Col &, const Col &,
+                                             const Col &, const Batch &,
+                                             int64_t) {}
+};
+
+// Net rate (fwd - rev) * pres_mod of any reaction: general rate forms,
+// pressure modification, non-integer coefficients.
+template <class CS>
+__device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
+                                          double mix, const CS &C, const CS &S,
+                                          double &fwd, double &rev, double &pm) {
+  double xf = 0.0;
+  const double kf = rate(t, r, s, xf);
+  fwd = kf * product(t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r], t.rx_ptr[r + 1], C);
+  const int j = t.rev_idx[r];
+  double net = fwd;
+  rev = 0.0;
+  if (j >= 0) {
+    double gsum = t.kc_lpref[j];
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e)
+      gsum = fma(t.nu_val[e], S[t.nu_sp[e]], gsum);
+    const double kr = (t.rate_kind[r] == RATE_EXP) ? exp_t(xf - gsum, s.tab)
+                                                   : kf * exp_t(-gsum, s.tab);
+    rev = kr * product(t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r], t.px_ptr[r + 1], C);
+    net = fwd - rev;
+  }
+  const int p = t.pm_idx[r];
+  pm = 1.0;
+  if (p >= 0) {
+    pm = pres_mod(t, p, s, mix, C);
+    net *= pm;
+  }
+  return net;
+}
+
+template <bool STAGES>
+__device__ __forceinline__ void general(const Tab &t, int r, const State &s,
+                                        double mix, const Col &C,
+                                        const Col &S, const Col &W,
+                                        const Batch &b, int64_t i) {
+  double fwd, rev, pm;
+  const double net = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+  if (STAGES) {
+    const int j = t.rev_idx[r], p = t.pm_idx[r];
+    if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
+    if (b.rev && j >= 0) b.rev[(int64_t)j * b.ld + i] = rev;
+    if (b.pm && p >= 0) b.pm[(int64_t)p * b.ld + i] = pm;
+  }
+  for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+    const int k = t.nu_sp[e];
+    W[k] = fma(t.nu_val[e], net, W[k]);
+  }
+}
+
+template <bool STAGES>
+__global__ void __launch_bounds__(128, 1)
+    k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  Tab t;
+  int nb;
+  if (!stage_ranges(smem, img, L, 0, &bar, b.status, t, nb)) return;
+  const int N = t.N;
+  double *base = reinterpret_cast<double *>(smem + nb);
+  const int64_t st = blockDim.x;
+  const Col C{base + threadIdx.x, st};
+  const Col W{base + (int64_t)N * st + threadIdx.x, st};
+  const Col S{base + (int64_t)2 * N * st + threadIdx.x, st};
+  int bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    State s;
+    s.T = b.T[i];
+    const double P = b.P[i];
+    s.invT = 1.0 / s.T;
+    s.logT = log(s.T);
+    s.tab = t.exptab;
+    // eval_conc
+    double ysum = 0.0, mwi = 0.0;
+    for (int k = 0; k < N - 1; ++k) {
+      const double y = b.Y[(int64_t)k * b.ld + i];
+      C[k] = y;
+      ysum += y;
+      mwi = fma(y, t.inv_mw[k], mwi);
+    }
+    const double yN = 1.0 - ysum;
+    mwi = fma(yN, t.inv_mw[N - 1], mwi);
+    const double rho = P / mwi * (s.invT * INV_RU);
+    for (int k = 0; k < N - 1; ++k) C[k] = C[k] * (rho * t.inv_mw[k]);
+    C[N - 1] = yN * (rho * t.inv_mw[N - 1]);
+    // per-species Gibbs terms and accumulators
+    for (int k = 0; k < N; ++k) {
+      const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
+      const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
+      double v = fma(h, s.T, g[0]);
+      v = fma(g[1], s.logT, v);
+      S[k] = fma(g[6], s.invT, v);
+      W[k] = 0.0;
+    }
+    if (STAGES && b.conc)
+      for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = C[k];
+    const double mix = P * s.invT * INV_RU;
+    Shapes<0, STAGES>::run(t, s, C, S, W, b, i);
+    for (int p = t.seg[NSHAPE]; p < t.R; ++p)
+      general<STAGES>(t, t.perm[p], s, mix, C, S, W, b, i);
+    for (int k = 0; k < N; ++k) {
+      const double v = W[k];
+      bad += !isfinite(v);
+      b.wdot[(int64_t)k * b.ld + i] = v;
+    }
+  }
+  if (bad && b.status) atomicAdd(&b.status[1], bad);
+}
+
+// ---- warp per state -----------------------------------------------------
+// A warp evaluates one state at a time: lanes split the species for the
+// concentrations and Gibbs terms, the reactions (in dperm order) for the
+// net rates, which go to a per-warp buffer q[R], and then the species
+// again -- balanced lane bins over the species-major CSR -- to sum wdot in
+// reaction order.  Per-state scalars (1/T, ln T) are computed once per
+// state by one lane of a 32-state batch.  With no per-thread arrays, many
+// more warps fit on an SM than with one state per thread.
+constexpr int DW = 8;  // warps per CTA
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <bool STAGES, bool SMEM_TAB>
+__global__ void __launch_bounds__(DW * 32)
+    k_wdot_warp(const unsigned char *__restrict__ img, ImgLayout L, Batch b,
+                int per_warp) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  int nb = 0;
+  Tab t;
+  if (SMEM_TAB) {
+    if (!stage_ranges(smem, img, L, 1, &bar, b.status, t, nb)) return;
+  } else {
+    t = make_tab(img, L);
+  }
+  const int N = t.N, R = t.R;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *wb = reinterpret_cast<double *>(smem + nb) + (size_t)warp * per_warp;
+  double *bT = wb, *bP = wb + 32, *biT = wb + 64, *blT = wb + 96;
+  const Arr C{wb + 128};
+  const Arr S{wb + 128 + N};
+  double *q = wb + 128 + 2 * N;
+  const int l0 = t.lane_ptr[lane], l1 = t.lane_ptr[lane + 1];
+  int bad = 0;
+  const int64_t nwarp = (int64_t)gridDim.x * DW;
+  for (int64_t i0 = ((int64_t)blockIdx.x * DW + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
+    // per-state scalars of a batch of 32 consecutive states, one per lane
+    {
+      const int64_t i = i0 + lane;
+      const double T = i < b.n ? b.T[i] : 1000.0;
+      bT[lane] = T;
+      bP[lane] = i < b.n ? b.P[i] : 101325.0;
+      biT[lane] = 1.0 / T;
+      blT[lane] = log(T);
+    }
+    __syncwarp();
+    const int jn = (b.n - i0) < 32 ? (int)(b.n - i0) : 32;
+    for (int j = 0; j < jn; ++j) {
+      const int64_t i = i0 + j;
+      State s;
+      s.T = bT[j];
+      s.invT = biT[j];
+      s.logT = blT[j];
+      s.tab = t.exptab;
+      const double P = bP[j];
+      // concentrations (lanes over species)
+      double ys = 0.0, mw = 0.0;
+      for (int k = lane; k < N - 1; k += 32) {
+        const double y = b.Y[(int64_t)k * b.ld + i];
+        C[k] = y;
+        ys += y;
+        mw = fma(y, t.inv_mw[k], mw);
+      }
+      ys = warp_sum(ys);
+      mw = warp_sum(mw);
+      const double yN = 1.0 - ys;
+      mw = fma(yN, t.inv_mw[N - 1], mw);
+      const double rho = P / mw * (s.invT * INV_RU);
+      __syncwarp();
+      for (int k = lane; k < N; k += 32) {
+        const double y = (k == N - 1) ? yN : C[k];
+        const double c = y * (rho * t.inv_mw[k]);
+        C[k] = c;
+        if (STAGES && b.conc) b.conc[(int64_t)k * b.ld + i] = c;
+        const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
+        const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
+        double v = fma(h, s.T, g[0]);
+        v = fma(g[1], s.logT, v);
+        S[k] = fma(g[6], s.invT, v);
+      }
+      __syncwarp();
+      // net rates (lanes over reactions)
+      const double mix = P * s.invT * INV_RU;
+      for (int p = lane; p < R; p += 32) {
+        const int r = t.dperm[p];
+        double fwd, rev, pm;
+        q[r] = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+        if (STAGES) {
+          const int jr = t.rev_idx[r], pp = t.pm_idx[r];
+          if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
+          if (b.rev && jr >= 0) b.rev[(int64_t)jr * b.ld + i] = rev;
+          if (b.pm && pp >= 0) b.pm[(int64_t)pp * b.ld + i] = pm;
+        }
+      }
+      __syncwarp();
+      // wdot (lanes over species, terms in reaction order)
+      for (int a = l0; a < l1; ++a) {
+        const int k = t.lane_sp[a];
+        double w = 0.0;
+        for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e)
+          w = fma(t.spc_nu[e], q[t.spc_r[e]], w);
+        bad += !isfinite(w);
+        b.wdot[(int64_t)k * b.ld + i] = w;
+      }
+      __syncwarp();
+    }
+  }
+  if (bad && b.status) atomicAdd(&b.status[1], bad);
+}
+
+}  // namespace fast
+
+int grid_for(int64_t n, int block, int max_ctas);
+
+// Thread-per-state variant (kept for comparison: CRS_MODE_FP64_TPS).
+cudaError_t launch_wdot_fp64_tps(const unsigned char *img, const ImgLayout &L,
+                                 const Batch &b, int sm_count, int smem_optin,
+                                 cudaStream_t s) {
+  const int block = 128;
+  const size_t tab = (size_t)(L.rng[0][1] - L.rng[0][0] + L.rng[0][3] - L.rng[0][2]);
+  const size_t bytes = tab + (size_t)3 * L.N * block * sizeof(double);
+  if (bytes > (size_t)smem_optin) return cudaErrorNotSupported;
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  auto k = stages ? fast::k_wdot<true> : fast::k_wdot<false>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wdot_fp64(const unsigned char *img, const ImgLayout &L,
+                             const Batch &b, int sm_count, int smem_optin,
+                             cudaStream_t s) {
+  const int per_warp = 128 + 2 * L.N + L.R + 1;  // doubles
+  const size_t warps = (size_t)fast::DW * per_warp * sizeof(double);
+  const size_t tab = (size_t)(L.rng[1][1] - L.rng[1][0] + L.rng[1][3] - L.rng[1][2]);
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  const int threads = fast::DW * 32;
+  const int64_t nbatch = (b.n + 31) / 32;
+  if (tab + warps <= (size_t)smem_optin) {
+    const size_t bytes = tab + warps;
+    auto k = stages ? fast::k_wdot_warp<true, true> : fast::k_wdot_warp<false, true>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, bytes);
+    const int grid = grid_for(nbatch, fast::DW, sm_count * (per_sm > 0 ? per_sm : 1));
+    k<<<grid, threads, bytes, s>>>(img, L, b, per_warp);
+  } else if (warps <= (size_t)smem_optin) {
+    auto k = stages ? fast::k_wdot_warp<true, false> : fast::k_wdot_warp<false, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warps);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, warps);
+    const int grid = grid_for(nbatch, fast::DW, sm_count * (per_sm > 0 ? per_sm : 1));
+    k<<<grid, threads, warps, s>>>(img, L, b, per_warp);
+  } else {
+    return cudaErrorNotSupported;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace crs

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace crs {
@@ -22,6 +23,28 @@ enum { STATUS_STAGE_TIMEOUT = 1 };
 struct ImgLayout {
   int N, R, NREV, NPM, NRATE, NKC;
   int bytes;  // image size, multiple of 16
+  // Byte ranges [lo, hi) of the image that each fast kernel stages into
+  // shared memory (two ranges per kernel, copied back to back); sections
+  // outside them are read from global memory through L1.
+  //   [0] FP64 one state per thread   [1] FP64 one state per warp
+  //   [2] mixed one state per thread  [3] mixed one state per warp
+  int rng[4][4];
+  // derived f64 sections (fast kernels): per rate row (logA, b, -Ta); per
+  // reversible reaction log(Kc prefactor); per pres_mod entry the Troe and
+  // SRI constants in multiply form; per species the 2x7 Gibbs
+  // coefficients; the 256-entry 2^(j/256) table of the exponential.
+  int rate_x, kc_lpref, troe_x, sri_x, sp_gibbs, exptab;
+  // derived f32 sections (mixed kernel): per rate row ln|A|, b, -Ta as
+  // float-float pairs and sign(A); 1/mw; Troe and SRI constants (exponent
+  // factors as float-float pairs); efficiencies minus one.
+  int rate_ff, inv_mw_f, troe_ff, sri_ff, eff_f;
+  // derived i32 sections: reaction processing order, start of each shape
+  // group in it (crs_shapes.cuh), expanded reactant / product factors
+  int perm, seg, rfac, pfac;
+  // warp-per-state kernels: reaction order (dperm), species-major net-nu
+  // CSR in reaction order (spc_ptr/spc_r/spc_nu), species per lane
+  // (lane_ptr/lane_sp)
+  int dperm, spc_ptr, spc_r, spc_nu, lane_ptr, lane_sp;
   // f64 sections
   int inv_mw, rate_par, rx_nu, px_nu, kc_tmid, kc_lo, kc_hi, kc_pref,
       pm_eff_val, pm_troe, pm_sri, nu_val, sp_tmid, sp_lo, sp_hi, kc_dnu;
@@ -33,6 +56,11 @@ struct ImgLayout {
 
 // Typed view of an image (in shared or global memory).
 struct Tab {
+  const int32_t *perm, *seg, *rfac, *pfac;
+  const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
+  const double *spc_nu;
+  const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
+  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab;
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
       *sp_hi, *kc_dnu;
@@ -43,11 +71,27 @@ struct Tab {
   int N, R, NREV, NPM;
 };
 
-__host__ __device__ inline Tab make_tab(const unsigned char *b,
-                                        const ImgLayout &L) {
+// View of an image whose byte ranges [lo, hi) and [lo2, hi2) have been
+// copied back to back to `near` (shared memory); every other section is
+// read at `far` (global memory).
+__host__ __device__ inline Tab make_tab2(const unsigned char *near,
+                                         const unsigned char *far,
+                                         const ImgLayout &L, int lo, int hi,
+                                         int lo2 = 0, int hi2 = 0) {
   Tab t;
-#define CRS_F(x) t.x = reinterpret_cast<const double *>(b + L.x)
-#define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(b + L.x)
+#define CRS_P(x)                                                      \
+  ((L.x >= lo && L.x < hi)     ? near + (L.x - lo)                    \
+   : (L.x >= lo2 && L.x < hi2) ? near + (hi - lo) + (L.x - lo2)       \
+                               : far + L.x)
+#define CRS_F(x) t.x = reinterpret_cast<const double *>(CRS_P(x))
+#define CRS_S(x) t.x = reinterpret_cast<const float *>(CRS_P(x))
+#define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
+  CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
+  CRS_F(exptab);
+  CRS_I(perm); CRS_I(seg); CRS_I(rfac); CRS_I(pfac);
+  CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
+  CRS_F(spc_nu);
+  CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
   CRS_F(inv_mw); CRS_F(rate_par); CRS_F(rx_nu); CRS_F(px_nu); CRS_F(kc_tmid);
   CRS_F(kc_lo); CRS_F(kc_hi); CRS_F(kc_pref); CRS_F(pm_eff_val);
   CRS_F(pm_troe); CRS_F(pm_sri); CRS_F(nu_val); CRS_F(sp_tmid); CRS_F(sp_lo);
@@ -57,11 +101,24 @@ __host__ __device__ inline Tab make_tab(const unsigned char *b,
   CRS_I(kc_ptr); CRS_I(pm_idx); CRS_I(pm_kind); CRS_I(pm_form); CRS_I(pm_sp);
   CRS_I(pm_eff_ptr); CRS_I(pm_eff_sp); CRS_I(pm_k0); CRS_I(pm_kinf);
   CRS_I(pm_troe_t2); CRS_I(pm_sri_de); CRS_I(nu_ptr); CRS_I(nu_sp);
+#undef CRS_P
 #undef CRS_F
+#undef CRS_S
 #undef CRS_I
   t.N = L.N; t.R = L.R; t.NREV = L.NREV; t.NPM = L.NPM;
   return t;
 }
+
+__host__ __device__ inline Tab make_tab(const unsigned char *b,
+                                        const ImgLayout &L) {
+  return make_tab2(b, b, L, 0, 0);
+}
+
+// A derived table computed on the host at load time.
+struct Derived {
+  int ImgLayout::*field;
+  std::vector<unsigned char> bytes;
+};
 
 // Arguments of one batched evaluation (device pointers, SoA with ld).
 struct Batch {
@@ -92,10 +149,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Stage `bytes` (multiple of 16, both pointers 16-byte aligned) from global
-// to shared memory.  Must be called by all threads of the CTA.  Returns
-// false (for every thread) when the copy did not complete in time.
+// to shared memory, followed by `bytes2` from `gsrc2` when given.  Must be
+// called by all threads of the CTA.  Returns false (for every thread) when
+// the copies did not complete in time.
 __device__ inline bool stage_to_smem(void *sdst, const void *gsrc, int bytes,
-                                     uint64_t *bar, int32_t *status) {
+                                     uint64_t *bar, int32_t *status,
+                                     const void *gsrc2 = nullptr,
+                                     int bytes2 = 0) {
   const uint32_t b = smem_u32(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
@@ -106,16 +166,21 @@ __device__ inline bool stage_to_smem(void *sdst, const void *gsrc, int bytes,
   if (threadIdx.x == 0) {
     asm volatile(
         "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
-        "r"(bytes)
+        "r"(bytes + bytes2)
         : "memory");
     const int CH = 32768;
-    for (int off = 0; off < bytes; off += CH) {
-      int sz = bytes - off < CH ? bytes - off : CH;
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-          "[%0], [%1], %2, [%3];" ::"r"(smem_u32(static_cast<char *>(sdst) + off)),
-          "l"(static_cast<const char *>(gsrc) + off), "r"(sz), "r"(b)
-          : "memory");
+    for (int part = 0; part < 2; ++part) {
+      const char *src = static_cast<const char *>(part ? gsrc2 : gsrc);
+      char *dst = static_cast<char *>(sdst) + (part ? bytes : 0);
+      const int nbytes = part ? bytes2 : bytes;
+      for (int off = 0; off < nbytes; off += CH) {
+        int sz = nbytes - off < CH ? nbytes - off : CH;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst + off)),
+            "l"(src + off), "r"(sz), "r"(b)
+            : "memory");
+      }
     }
   }
   bool done = false;
@@ -130,6 +195,21 @@ __device__ inline bool stage_to_smem(void *sdst, const void *gsrc, int bytes,
   if (!all && threadIdx.x == 0 && status) atomicOr(&status[0], STATUS_STAGE_TIMEOUT);
   return all != 0;
 }
+
+// Stage ranges r of the image into shared memory and return the view.
+__device__ inline bool stage_ranges(unsigned char *smem,
+                                    const unsigned char *img,
+                                    const ImgLayout &L, int r, uint64_t *bar,
+                                    int32_t *status, Tab &t, int &nbytes) {
+  const int *g = L.rng[r];
+  nbytes = (g[1] - g[0]) + (g[3] - g[2]);
+  if (!stage_to_smem(smem, img + g[0], g[1] - g[0], bar, status, img + g[2],
+                     g[3] - g[2]))
+    return false;
+  t = make_tab2(smem, img, L, g[0], g[1], g[2], g[3]);
+  return true;
+}
+
 #endif
 
 }  // namespace crs

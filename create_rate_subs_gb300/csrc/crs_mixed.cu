@@ -1,0 +1,652 @@
+// CRS_MODE_MIXED: FP32 bulk arithmetic, FP64 where stability needs it.
+//
+// FP64 instructions are kept for
+//   * the per-species Gibbs terms S_k and, per reaction, the exponent of
+//     the equilibrium constant sum_k nu_k S_k + ln(prefactor);
+//   * the net rate fwd - rev (cancels near equilibrium);
+//   * the accumulation of wdot;
+//   * per-state scalars (1/T, ln T, the mass-fraction sums behind rho).
+// Everything else runs on the FP32 pipe, which on GB300 issues ~70x more
+// operations per clock than the FP64 pipe:
+//   * Arrhenius exponents ln|A| + b ln T - Ta/T as float-float pairs
+//     (~44 significant bits), so that |x| up to ~300 keeps an absolute
+//     error near 1e-12;
+//   * exp(x) = 2^k exp(r): Cody-Waite reduction in FP32 with a 16-bit
+//     ln2 head (exact through fmaf), r in [-ln2/2, ln2/2], degree-7 Taylor
+//     polynomial (truncation 6e-9);
+//   * rates kept as an FP32 mantissa times 2^E with an integer E, so that
+//     rates far outside the FP32 range (1/Kc can reach e^150 with random
+//     thermochemistry) neither overflow nor underflow; the FP64 value is
+//     assembled with integer operations only;
+//   * concentrations, third-body sums and fall-off broadening in FP32.
+// The error against FP64, scaled by the gross rate of each species, is
+// measured by the tests and reported by bench.py.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "crs_internal.cuh"
+#include "crs_shapes.cuh"
+
+namespace crs {
+namespace mixed {
+
+constexpr float LOG2E_F = 1.4426950216293335f;
+constexpr float LN2_HI_F = 0.693145751953125f;  // 16 significant bits
+constexpr float LN2_LO_F = 1.428606765330187e-06f;
+constexpr float SHIFT_F = 12582912.0f;          // 1.5 * 2^23
+constexpr double INV_RU = 0.0001202723625380408;
+constexpr float LN10_F = 2.302585092994046f;
+constexpr float INV_LN10_F = 0.4342944819032518f;
+
+struct ff {
+  float h, l;
+};
+
+__device__ __forceinline__ ff ff_norm(float s, float e) {
+  const float h = s + e;
+  return ff{h, e - (h - s)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  float e = (a.h - (s - bb)) + (b.h - bb);
+  e += a.l + b.l;
+  return ff_norm(s, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return ff_norm(p, e);
+}
+
+// exact float -> double for normal numbers, by integer operations
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// double -> float, round to nearest even, by integer operations when the
+// result is a normal float
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return __double2float_rn(d);
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  unsigned u = (hi & 0x80000000u) | ((unsigned)e << 23) | mant;
+  u += (rest > 0x10000000u) || (rest == 0x10000000u && (mant & 1u));
+  return __uint_as_float(u);
+}
+
+__device__ __forceinline__ ff ff_from_double(double d) {
+  const float h = d2f_rn(d);
+  return ff{h, d2f_rn(d - f2d_exact(h))};
+}
+
+// value m * 2^E as a double, by integer operations; m is an FP32 number
+// whose magnitude stays within [2^-8, 2^8] or is zero / non-finite
+__device__ __forceinline__ double assemble(float m, int E) {
+  const unsigned u = __float_as_uint(m);
+  const int fe = (int)((u >> 23) & 0xffu);
+  if (fe == 0) return 0.0;
+  if (fe == 0xff) return (double)m;
+  const int de = fe - 127 + 1023 + E;
+  if (de <= 0) return 0.0;
+  if (de >= 2047) return (u >> 31) ? -INFINITY : INFINITY;
+  const unsigned hi = (u & 0x80000000u) | ((unsigned)de << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// exp(x) for a float-float x, as (p, k) with exp(x) = p * 2^k,
+// p in [0.70, 1.42]
+__device__ __forceinline__ float ff_exp(ff x, int &k) {
+  if (!(fabsf(x.h) <= 3.0e3f)) {  // far outside the FP64 range, or NaN
+    if (x.h != x.h) {
+      k = 0;
+      return x.h;
+    }
+    x.h = copysignf(3.0e3f, x.h);
+    x.l = 0.0f;
+  }
+  const float t = fmaf(x.h, LOG2E_F, SHIFT_F);
+  const float kf = t - SHIFT_F;
+  k = __float_as_int(t) - 0x4b400000;
+  float r = fmaf(kf, -LN2_HI_F, x.h);
+  r = fmaf(kf, -LN2_LO_F, r);
+  r = r + x.l;
+  float p = fmaf(r, 1.0f / 5040.0f, 1.0f / 720.0f);
+  p = fmaf(p, r, 1.0f / 120.0f);
+  p = fmaf(p, r, 1.0f / 24.0f);
+  p = fmaf(p, r, 1.0f / 6.0f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  return fmaf(p, r, 1.0f);
+}
+
+// exp of a float-float argument as a plain float (saturating)
+__device__ __forceinline__ float ff_expf(ff x) {
+  if (x.h > 88.0f) return INFINITY;
+  if (x.h < -103.0f) return 0.0f;
+  int k;
+  const float p = ff_exp(x, k);
+  return ldexpf(p, k);
+}
+
+// split a float into mantissa in [1,2) (sign kept) and exponent; zero and
+// subnormal values give m = 0
+__device__ __forceinline__ float fsplit(float c, int &e) {
+  const unsigned u = __float_as_uint(c);
+  const unsigned fe = (u >> 23) & 0xffu;
+  e = (int)fe - 127;
+  if (fe == 0u) {
+    e = 0;
+    return 0.0f;
+  }
+  return __uint_as_float((u & 0x807fffffu) | 0x3f800000u);
+}
+
+struct FCol {
+  float *p;
+  int stride;
+  __device__ float &operator[](int k) const { return p[k * stride]; }
+};
+struct DCol {
+  double *p;
+  int stride;
+  __device__ double &operator[](int k) const { return p[k * stride]; }
+};
+
+// Contiguous per-warp arrays (warp-per-state kernel).
+struct FArr {
+  float *p;
+  __device__ float &operator[](int k) const { return p[k]; }
+};
+struct DArr {
+  double *p;
+  __device__ double &operator[](int k) const { return p[k]; }
+};
+
+struct State {
+  double T, invT, logT;
+  float Tf;
+  ff Tff, lTff, iTff;
+};
+
+// Arrhenius exponent of a rate row as float-float, and the sign of A.
+__device__ __forceinline__ ff rate_exponent(const Tab &t, int row,
+                                            const State &s, float &sign) {
+  const float *c = t.rate_ff + 8 * row;
+  ff x = ff_add(ff{c[0], c[1]}, ff_mul(ff{c[2], c[3]}, s.lTff));
+  x = ff_add(x, ff_mul(ff{c[4], c[5]}, s.iTff));
+  sign = c[6];
+  return x;
+}
+
+// product of concentration factors as mantissa * 2^E
+template <class FC>
+__device__ __forceinline__ float product(const int32_t *sp, const int32_t *nint,
+                                         const double *nu, int a, int b,
+                                         const FC &C, int &E) {
+  float m = 1.0f;
+  for (int j = a; j < b; ++j) {
+    const float c = C[sp[j]];
+    int n = nint[j];
+    if (n < 0) {
+      int e;
+      const float f = fsplit(powf(c, (float)nu[j]), e);
+      m *= f;
+      E += e;
+      continue;
+    }
+    int e;
+    const float f = fsplit(c, e);
+    for (; n > 0; --n) {
+      m *= f;
+      E += e;
+      // keep the mantissa product inside [2^-8, 2^8]
+      int e2;
+      m = fsplit(m, e2);
+      E += e2;
+    }
+  }
+  return m;
+}
+
+// pres_mod entry p in FP32.  The reduced pressure enters through
+// ln Pr = (x_0 - x_inf) + ln [M], so that it never overflows.
+template <class FC>
+__device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
+                          const FC &C) {
+  float thd = mix;
+  const int sp = t.pm_sp[p];
+  if (t.pm_kind[p] == PM_THD || sp < 0) {
+    for (int e = t.pm_eff_ptr[p]; e < t.pm_eff_ptr[p + 1]; ++e)
+      thd = fmaf(t.eff_f[e], C[t.pm_eff_sp[e]], thd);
+    if (t.pm_kind[p] == PM_THD) return thd;
+  } else {
+    thd = C[sp];
+  }
+  float sg0, sgi;
+  const ff x0 = rate_exponent(t, t.pm_k0[p], s, sg0);
+  const ff xi = rate_exponent(t, t.pm_kinf[p], s, sgi);
+  // Pr = exp(x_0 - x_inf) * [M] as mantissa * 2^E: no overflow, and the
+  // float-float exponent difference keeps its precision
+  int E;
+  const float pe = ff_exp(ff_add(x0, ff_neg(xi)), E);
+  int et;
+  const float mt = fsplit(thd * sg0 * sgi, et);
+  float m = pe * mt;
+  E += et;
+  int e2;
+  m = fsplit(m, e2);
+  E += e2;
+  const bool low = t.pm_kind[p] == PM_FALL_LOW;
+  float frac, inv1p;  // Pr/(1+Pr), 1/(1+Pr)
+  if (m <= 0.0f) {
+    frac = 0.0f;
+    inv1p = 1.0f;
+  } else if (E >= 0) {
+    const float q = ldexpf(1.0f / m, -E);  // 1/Pr <= 1
+    frac = 1.0f / (1.0f + q);
+    inv1p = q * frac;
+  } else {
+    const float pr = ldexpf(m, E);  // Pr < 1
+    inv1p = 1.0f / (1.0f + pr);
+    frac = pr * inv1p;
+  }
+  // ln Pr for the broadening functions (only its log is needed there)
+  const float lnPr = (m > 0.0f) ? (float)E * 0.6931471805599453f + logf(m) : -1.0e30f;
+  const int form = t.pm_form[p];
+  if (form == FORM_LINDEMANN) return low ? frac : inv1p;
+  // log10(fmax(Pr, 1e-300))
+  const float lP = fmaxf(lnPr * INV_LN10_F, -300.0f);
+  float F;
+  if (form == FORM_TROE) {
+    const float *c = t.troe_ff + 8 * p;  // P0, -1/T3 (ff), P2, -1/T1 (ff), -T2 (ff)
+    float f = c[0] * ff_expf(ff_mul(s.Tff, ff{c[1], c[2]})) +
+              c[3] * ff_expf(ff_mul(s.Tff, ff{c[4], c[5]}));
+    if (t.pm_troe_t2[p]) f += ff_expf(ff_mul(s.iTff, ff{c[6], c[7]}));
+    const float lF = log10f(fmaxf(f, 1.0e-37f));
+    const float A = lP - 0.67f * lF - 0.4f;
+    const float B = 0.806f - 1.1762f * lF - 0.14f * lP;
+    F = expf(LN10_F * lF / (1.0f + A * A / (B * B)));
+  } else {
+    const float *c = t.sri_ff + 8 * p;  // a, -b (ff), -1/c (ff), d, e
+    const float X = 1.0f / (1.0f + lP * lP);
+    const float base = c[0] * ff_expf(ff_mul(s.iTff, ff{c[1], c[2]})) +
+                       ff_expf(ff_mul(s.Tff, ff{c[3], c[4]}));
+    F = expf(X * logf(base));
+    if (t.pm_sri_de[p]) F *= c[5] * expf(c[6] * (s.lTff.h + s.lTff.l));
+  }
+  return low ? F * frac : F * inv1p;
+}
+
+template <int NR, int NP, int NNU, int REV, bool STAGES>
+__device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
+                                            int cnt, const State &s,
+                                            const FCol &C, const DCol &S,
+                                            const DCol &W, const Batch &b,
+                                            int64_t i) {
+  ff x[4];
+  double fwd[4], rev[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int r = rr[u];
+    float sg;
+    x[u] = rate_exponent(t, r, s, sg);
+    int E;
+    float m = ff_exp(x[u], E);
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      int e;
+      m *= fsplit(C[t.rfac[MAXF * r + q]], e);
+      E += e;
+    }
+    fwd[u] = assemble(m, E);
+    rev[u] = 0.0;
+  }
+  if (REV) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = rr[u];
+      const int e0 = t.nu_ptr[r];
+      double g = t.kc_lpref[t.rev_idx[r]];  // Kc exponent in FP64
+#pragma unroll
+      for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], S[t.nu_sp[e0 + q]], g);
+      int E;
+      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double(g))), E);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        int e;
+        m *= fsplit(C[t.pfac[MAXF * r + q]], e);
+        E += e;
+      }
+      rev[u] = assemble(m, E);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (u >= cnt) break;
+    const int r = rr[u];
+    const double net = fwd[u] - rev[u];  // FP64
+    if (STAGES) {
+      if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd[u];
+      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[r] * b.ld + i] = rev[u];
+    }
+    const int e0 = t.nu_ptr[r];
+#pragma unroll
+    for (int q = 0; q < NNU; ++q) {
+      const int k = t.nu_sp[e0 + q];
+      W[k] = fma(t.nu_val[e0 + q], net, W[k]);  // FP64 accumulation
+    }
+  }
+}
+
+template <int SH, bool STAGES>
+struct Shapes {
+  __device__ __forceinline__ static void run(const Tab &t, const State &s,
+                                             const FCol &C, const DCol &S,
+                                             const DCol &W, const Batch &b,
+                                             int64_t i) {
+    constexpr Shape d = shape_of(SH);
+    const int p0 = t.seg[SH], p1 = t.seg[SH + 1];
+    for (int p = p0; p < p1; p += 4) {
+      const int cnt = p1 - p < 4 ? p1 - p : 4;
+      int rr[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) rr[u] = t.perm[p + (u < cnt ? u : cnt - 1)];
+      shape_block<d.nr, d.np, d.nnu, d.rev, STAGES>(t, rr, cnt, s, C, S, W, b, i);
+    }
+    Shapes<SH + 1, STAGES>::run(t, s, C, S, W, b, i);
+  }
+};
+template <bool STAGES>
+struct Shapes<NSHAPE, STAGES> {
+  __device__ __forceinline__ static void run(const Tab &, const State &,
+                                             const FCol &, const DCol &,
+                                             const DCol &, const Batch &,
+                                             int64_t) {}
+};
+
+// Net rate (fwd - rev) * pres_mod of any reaction, as FP64.
+template <class FC, class DC>
+__device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
+                                          float mix, const FC &C, const DC &S,
+                                          double &fwd, double &rev, float &pm) {
+  float sgn;
+  const ff xf = rate_exponent(t, r, s, sgn);
+  int Ef;
+  const float pf = ff_exp(xf, Ef);
+  const float mf = sgn * pf * product(t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
+                                      t.rx_ptr[r + 1], C, Ef);
+  fwd = assemble(mf, Ef);
+  const int j = t.rev_idx[r];
+  double net = fwd;
+  rev = 0.0;
+  if (j >= 0) {
+    double g = t.kc_lpref[j];  // Kc exponent in FP64
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e)
+      g = fma(t.nu_val[e], S[t.nu_sp[e]], g);
+    int Er;
+    const float pr = ff_exp(ff_add(xf, ff_neg(ff_from_double(g))), Er);
+    const float mr = sgn * pr * product(t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r],
+                                        t.px_ptr[r + 1], C, Er);
+    rev = assemble(mr, Er);
+    net = fwd - rev;  // FP64
+  }
+  const int p = t.pm_idx[r];
+  pm = 1.0f;
+  if (p >= 0) {
+    pm = pres_mod(t, p, s, mix, C);
+    net *= f2d_exact(pm);
+  }
+  return net;
+}
+
+template <bool STAGES>
+__device__ __forceinline__ void general(const Tab &t, int r, const State &s,
+                                        float mix, const FCol &C,
+                                        const DCol &S, const DCol &W,
+                                        const Batch &b, int64_t i) {
+  double fwd, rev;
+  float pm;
+  const double net = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+  if (STAGES) {
+    const int j = t.rev_idx[r], p = t.pm_idx[r];
+    if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
+    if (b.rev && j >= 0) b.rev[(int64_t)j * b.ld + i] = rev;
+    if (b.pm && p >= 0) b.pm[(int64_t)p * b.ld + i] = (double)pm;
+  }
+  for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+    const int k = t.nu_sp[e];
+    W[k] = fma(t.nu_val[e], net, W[k]);  // FP64 accumulation
+  }
+}
+
+template <bool STAGES>
+__global__ void __launch_bounds__(128, 1)
+    k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  Tab t;
+  int nb;
+  if (!stage_ranges(smem, img, L, 2, &bar, b.status, t, nb)) return;
+  const int N = t.N;
+  const int st = blockDim.x;
+  double *dbase = reinterpret_cast<double *>(smem + nb);
+  const DCol W{dbase + threadIdx.x, st};
+  const DCol S{dbase + N * st + threadIdx.x, st};
+  const FCol C{reinterpret_cast<float *>(dbase + 2 * N * st) + threadIdx.x, st};
+  int bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    State s;
+    s.T = b.T[i];
+    const double P = b.P[i];
+    s.invT = 1.0 / s.T;
+    s.logT = log(s.T);
+    s.Tf = (float)s.T;
+    s.Tff = ff_from_double(s.T);
+    s.lTff = ff_from_double(s.logT);
+    s.iTff = ff_from_double(s.invT);
+    // concentrations: sums and C = y * (rho / mw) in FP64, each C rounded
+    // once to FP32
+    double ysum = 0.0, mwi = 0.0;
+    for (int k = 0; k < N - 1; ++k) {
+      const double y = b.Y[(int64_t)k * b.ld + i];
+      ysum += y;
+      mwi = fma(y, t.inv_mw[k], mwi);
+    }
+    const double yN = 1.0 - ysum;
+    mwi = fma(yN, t.inv_mw[N - 1], mwi);
+    const double rho = P / mwi * (s.invT * INV_RU);
+    for (int k = 0; k < N - 1; ++k)
+      C[k] = d2f_rn(b.Y[(int64_t)k * b.ld + i] * (rho * t.inv_mw[k]));
+    C[N - 1] = d2f_rn(yN * (rho * t.inv_mw[N - 1]));
+    // FP64 Gibbs terms
+    for (int k = 0; k < N; ++k) {
+      const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
+      const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
+      double v = fma(h, s.T, g[0]);
+      v = fma(g[1], s.logT, v);
+      S[k] = fma(g[6], s.invT, v);
+      W[k] = 0.0;
+    }
+    if (STAGES && b.conc)
+      for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = (double)C[k];
+    const float mix = d2f_rn(P * s.invT * INV_RU);
+    Shapes<0, STAGES>::run(t, s, C, S, W, b, i);
+    for (int p = t.seg[NSHAPE]; p < t.R; ++p)
+      general<STAGES>(t, t.perm[p], s, mix, C, S, W, b, i);
+    for (int k = 0; k < N; ++k) {
+      const double v = W[k];
+      bad += !isfinite(v);
+      b.wdot[(int64_t)k * b.ld + i] = v;
+    }
+  }
+  if (bad && b.status) atomicAdd(&b.status[1], bad);
+}
+
+// ---- warp per state (see crs_fast.cu for the layout) --------------------
+constexpr int DW = 8;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <bool STAGES, bool SMEM_TAB>
+__global__ void __launch_bounds__(DW * 32)
+    k_wdot_warp(const unsigned char *__restrict__ img, ImgLayout L, Batch b,
+                int per_warp) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  int nb = 0;
+  Tab t;
+  if (SMEM_TAB) {
+    if (!stage_ranges(smem, img, L, 3, &bar, b.status, t, nb)) return;
+  } else {
+    t = make_tab(img, L);
+  }
+  const int N = t.N, R = t.R;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *wb = reinterpret_cast<double *>(smem + nb) + (size_t)warp * per_warp;
+  double *bT = wb, *bP = wb + 32, *biT = wb + 64, *blT = wb + 96;
+  const DArr S{wb + 128};
+  double *q = wb + 128 + N;
+  const FArr C{reinterpret_cast<float *>(wb + 128 + N + R)};
+  const int l0 = t.lane_ptr[lane], l1 = t.lane_ptr[lane + 1];
+  int bad = 0;
+  const int64_t nwarp = (int64_t)gridDim.x * DW;
+  for (int64_t i0 = ((int64_t)blockIdx.x * DW + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
+    {
+      const int64_t i = i0 + lane;
+      const double T = i < b.n ? b.T[i] : 1000.0;
+      bT[lane] = T;
+      bP[lane] = i < b.n ? b.P[i] : 101325.0;
+      biT[lane] = 1.0 / T;
+      blT[lane] = log(T);
+    }
+    __syncwarp();
+    const int jn = (b.n - i0) < 32 ? (int)(b.n - i0) : 32;
+    for (int j = 0; j < jn; ++j) {
+      const int64_t i = i0 + j;
+      State s;
+      s.T = bT[j];
+      s.invT = biT[j];
+      s.logT = blT[j];
+      s.Tf = (float)s.T;
+      s.Tff = ff_from_double(s.T);
+      s.lTff = ff_from_double(s.logT);
+      s.iTff = ff_from_double(s.invT);
+      const double P = bP[j];
+      double ys = 0.0, mw = 0.0;
+      for (int k = lane; k < N - 1; k += 32) {
+        const double y = b.Y[(int64_t)k * b.ld + i];
+        ys += y;
+        mw = fma(y, t.inv_mw[k], mw);
+      }
+      ys = warp_sum(ys);
+      mw = warp_sum(mw);
+      const double yN = 1.0 - ys;
+      mw = fma(yN, t.inv_mw[N - 1], mw);
+      const double rho = P / mw * (s.invT * INV_RU);
+      for (int k = lane; k < N; k += 32) {
+        const double y = (k == N - 1) ? yN : b.Y[(int64_t)k * b.ld + i];
+        const float c = d2f_rn(y * (rho * t.inv_mw[k]));
+        C[k] = c;
+        if (STAGES && b.conc) b.conc[(int64_t)k * b.ld + i] = (double)c;
+        const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
+        const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
+        double v = fma(h, s.T, g[0]);
+        v = fma(g[1], s.logT, v);
+        S[k] = fma(g[6], s.invT, v);  // FP64 Gibbs term
+      }
+      __syncwarp();
+      const float mix = d2f_rn(P * s.invT * INV_RU);
+      for (int p = lane; p < R; p += 32) {
+        const int r = t.dperm[p];
+        double fwd, rev;
+        float pm;
+        q[r] = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+        if (STAGES) {
+          const int jr = t.rev_idx[r], pp = t.pm_idx[r];
+          if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
+          if (b.rev && jr >= 0) b.rev[(int64_t)jr * b.ld + i] = rev;
+          if (b.pm && pp >= 0) b.pm[(int64_t)pp * b.ld + i] = (double)pm;
+        }
+      }
+      __syncwarp();
+      for (int a = l0; a < l1; ++a) {
+        const int k = t.lane_sp[a];
+        double w = 0.0;
+        for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e)
+          w = fma(t.spc_nu[e], q[t.spc_r[e]], w);  // FP64 accumulation
+        bad += !isfinite(w);
+        b.wdot[(int64_t)k * b.ld + i] = w;
+      }
+      __syncwarp();
+    }
+  }
+  if (bad && b.status) atomicAdd(&b.status[1], bad);
+}
+
+}  // namespace mixed
+
+int grid_for(int64_t n, int block, int max_ctas);
+
+// Thread-per-state variant (kept for comparison: CRS_MODE_MIXED_TPS).
+cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
+                                  const Batch &b, int sm_count, int smem_optin,
+                                  cudaStream_t s) {
+  const int block = 128;
+  const size_t tab = (size_t)(L.rng[2][1] - L.rng[2][0] + L.rng[2][3] - L.rng[2][2]);
+  const size_t cols = (size_t)L.N * block * (8 + 8 + 4);
+  if (tab + cols > (size_t)smem_optin) return cudaErrorNotSupported;
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  auto k = stages ? mixed::k_wdot<true> : mixed::k_wdot<false>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(tab + cols));
+  k<<<grid_for(b.n, block, sm_count), block, tab + cols, s>>>(img, L, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wdot_mixed(const unsigned char *img, const ImgLayout &L,
+                              const Batch &b, int sm_count, int smem_optin,
+                              cudaStream_t s) {
+  // doubles: 4 x 32 scalars, S[N], q[R], then C[N] as floats
+  const int per_warp = 128 + L.N + L.R + (L.N + 1) / 2 + 1;
+  const size_t warps = (size_t)mixed::DW * per_warp * sizeof(double);
+  const size_t tab = (size_t)(L.rng[3][1] - L.rng[3][0] + L.rng[3][3] - L.rng[3][2]);
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  const int threads = mixed::DW * 32;
+  const int64_t nbatch = (b.n + 31) / 32;
+  if (tab + warps <= (size_t)smem_optin) {
+    const size_t bytes = tab + warps;
+    auto k = stages ? mixed::k_wdot_warp<true, true> : mixed::k_wdot_warp<false, true>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, bytes);
+    const int grid = grid_for(nbatch, mixed::DW, sm_count * (per_sm > 0 ? per_sm : 1));
+    k<<<grid, threads, bytes, s>>>(img, L, b, per_warp);
+  } else if (warps <= (size_t)smem_optin) {
+    auto k = stages ? mixed::k_wdot_warp<true, false> : mixed::k_wdot_warp<false, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warps);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, warps);
+    const int grid = grid_for(nbatch, mixed::DW, sm_count * (per_sm > 0 ? per_sm : 1));
+    k<<<grid, threads, warps, s>>>(img, L, b, per_warp);
+  } else {
+    return cudaErrorNotSupported;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace crs

@@ -47,6 +47,13 @@ typedef struct crs_mech crs_mech;
 #define CRS_MODE_FP64 0        /* FP64 throughout; <=1e-12 of the reference */
 #define CRS_MODE_FP64_STRICT 1 /* FP64 in the reference's operation order */
 #define CRS_MODE_MIXED 2       /* FP32 bulk, FP64 Kc exponent/net rate/sum */
+/* The arithmetic of CRS_MODE_FP64 / CRS_MODE_MIXED with a fixed thread
+ * layout: one state per thread (TPS) or one state per warp (WARP).  The
+ * default modes pick the faster layout that fits the mechanism. */
+#define CRS_MODE_FP64_TPS 3
+#define CRS_MODE_MIXED_TPS 4
+#define CRS_MODE_FP64_WARP 5
+#define CRS_MODE_MIXED_WARP 6
 
 /* ---- mechanism tables ------------------------------------------------ */
 
@@ -56,6 +63,11 @@ typedef struct crs_mech crs_mech;
  * code (rate_subs.py:226-1391). */
 int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out);
 int crs_mech_load_file(const char *path, crs_mech **out);
+/* Validate a blob and report, without touching a GPU: out[0] device table
+ * bytes, out[1] / out[2] bytes the FP64 / mixed kernels stage into shared
+ * memory, out[3] / out[4] / out[5] shared memory per 128-thread CTA of
+ * CRS_MODE_FP64 / CRS_MODE_MIXED / CRS_MODE_FP64_STRICT (all on chip). */
+int crs_mech_inspect(const void *blob, size_t nbytes, int64_t out[6]);
 int crs_mech_free(crs_mech *mech);
 /* out[0..4] = species, reactions, reversible reactions, pres_mod entries,
  * rate-constant rows. */
