@@ -18,7 +18,7 @@ enum { PM_THD = 0, PM_FALL_LOW = 1, PM_FALL_HIGH = 2 };
 enum { FORM_LINDEMANN = 0, FORM_TROE = 1, FORM_SRI = 2 };
 
 // Status word bits (device, one per mechanism handle).
-enum { STATUS_STAGE_TIMEOUT = 1 };
+enum { STATUS_STAGE_TIMEOUT = 1, STATUS_GEMM_TIMEOUT = 2 };
 
 struct ImgLayout {
   int N, R, NREV, NPM, NRATE, NKC;

@@ -75,7 +75,8 @@ int crs_mech_dims(const crs_mech *mech, int64_t out[5]);
 const char *crs_last_error(void);
 /* Non-finite outputs and device-wait timeouts recorded since the last
  * crs_status_reset on this handle: out[0] = flag bits (1 = table staging
- * timed out), out[1] = count of non-finite wdot values.  Synchronises
+ * timed out, 2 = a tensor-core GEMM wait timed out), out[1] = count of
+ * non-finite wdot values.  Synchronises
  * `stream`. */
 int crs_status(const crs_mech *mech, void *stream, int32_t out[2]);
 int crs_status_reset(const crs_mech *mech, void *stream);
@@ -118,6 +119,17 @@ int crs_wdot_stages(const crs_mech *mech, int64_t n, const double *T,
                     const double *P, const double *Y, int64_t ld,
                     double *wdot, double *conc, double *fwd, double *rev,
                     double *pres_mod, int mode, void *stream);
+
+/* ---- building blocks (no counterpart in the reference) ----------------- */
+
+/* D[m*ldd + n] = sum_k A[m*K + k] * B[n*K + k]: bf16 inputs (device,
+ * row-major, K contiguous), fp32 output, on the tensor cores (tcgen05, TMA
+ * operand staging).  M a multiple of 128, K of 64, N of block_n, block_n in
+ * {64, 128, 192, 256}.  status (may be NULL): device int32[2], bit 2 of
+ * status[0] is set when a bounded device wait expires. */
+int crs_gemm_bf16(const void *A, const void *B, float *D, int64_t M, int64_t N,
+                  int64_t K, int64_t ldd, int block_n, int32_t *status,
+                  void *stream);
 
 /* ---- measurement helper (no counterpart in the reference) ------------- */
 
