@@ -6,9 +6,12 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
+
+#include <cuda_bf16.h>
 
 #include "../../include/crs.h"
 #include "crs_internal.cuh"
@@ -32,6 +35,13 @@ cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
 cudaError_t launch_stage(int which, const unsigned char *img,
                          const ImgLayout &L, const Batch &b, double *y_N,
                          double *mw, double *rho, int sm_count, cudaStream_t s);
+cudaError_t launch_wdot_mixed_q(const unsigned char *img, const ImgLayout &L,
+                                const Batch &b, int sm_count, int smem_optin,
+                                cudaStream_t s, const mixed::QOut &qo);
+cudaError_t launch_gemm_wdot(const void *A, const void *B, int64_t M_pad, int64_t N_pad,
+                             int64_t K, int block_n, double *out, int64_t ld, int m_valid,
+                             int n_valid, const int *escale, int32_t *status,
+                             cudaStream_t s);
 // Tables the fast kernels derive from the blob's tables at load time.
 bool build_fast_tables(const std::vector<unsigned char> &img,
                        const ImgLayout &L, std::vector<Derived> &extra);
@@ -45,6 +55,17 @@ struct crs_mech {
   unsigned char *d_img = nullptr;  // device table image
   int32_t *d_status = nullptr;     // [0] flags, [1] non-finite count
   std::vector<unsigned char> h_img;
+  // tensor-core contraction (CRS_MODE_GEMM): nu as a bf16 matrix
+  // [N_pad][2*Kh] (each row nu_k, then nu_k again for the lo half), and a
+  // workspace for one chunk of states (bf16 rows + per-state exponents),
+  // allocated on first use and reused by later calls
+  std::mutex ws_mu;
+  int gemm_state = 0;  // 0 unknown, 1 ready, -1 unsupported
+  int Kh = 0, N_pad = 0, block_n = 64;
+  void *d_nuB = nullptr;
+  void *d_ws = nullptr;
+  int *d_escale = nullptr;
+  int64_t ws_rows = 0;
 };
 
 namespace {
@@ -333,6 +354,77 @@ crs::Batch make_batch(const crs_mech *m, int64_t n, int64_t ld) {
   return b;
 }
 
+// Chunk of states per contraction pass (workspace rows).
+constexpr int64_t GEMM_CHUNK = 1 << 18;
+
+int gemm_prepare(crs_mech *m) {
+  if (m->gemm_state) return m->gemm_state > 0 ? CRS_OK : CRS_ERR_UNSUPPORTED;
+  const crs::ImgLayout &L = m->L;
+  const crs::Tab t = crs::make_tab(m->h_img.data(), L);
+  m->Kh = (L.R + 63) / 64 * 64;
+  m->block_n = L.N <= 64 ? 64 : L.N <= 128 ? 128 : L.N <= 192 ? 192 : L.N <= 256 ? 256 : 192;
+  m->N_pad = (L.N + m->block_n - 1) / m->block_n * m->block_n;
+  const int64_t K = 2 * (int64_t)m->Kh;
+  std::vector<__nv_bfloat16> B((size_t)m->N_pad * K, __float2bfloat16(0.0f));
+  for (int r = 0; r < L.R; ++r)
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+      const double nu = t.nu_val[e];
+      const __nv_bfloat16 v = __float2bfloat16((float)nu);
+      if ((double)__bfloat162float(v) != nu) {
+        m->gemm_state = -1;
+        return fail(CRS_ERR_UNSUPPORTED,
+                    "a stoichiometric coefficient is not exact in bf16 (reaction %d)", r);
+      }
+      const int k = t.nu_sp[e];
+      B[(size_t)k * K + r] = v;
+      B[(size_t)k * K + m->Kh + r] = v;
+    }
+  cudaError_t e = cudaMalloc(&m->d_nuB, B.size() * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->d_nuB, B.data(), B.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "gemm tables");
+  m->gemm_state = 1;
+  return CRS_OK;
+}
+
+int wdot_gemm(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(m->ws_mu);
+  int rc = gemm_prepare(m);
+  if (rc != CRS_OK) return rc;
+  const int64_t K = 2 * (int64_t)m->Kh;
+  const int64_t rows = std::min<int64_t>((b.n + 127) / 128 * 128, GEMM_CHUNK);
+  if (m->ws_rows < rows) {
+    if (m->d_ws) cudaFree(m->d_ws);
+    if (m->d_escale) cudaFree(m->d_escale);
+    m->d_ws = nullptr;
+    m->d_escale = nullptr;
+    m->ws_rows = 0;
+    cudaError_t e = cudaMalloc(&m->d_ws, (size_t)rows * K * sizeof(__nv_bfloat16));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_escale, (size_t)rows * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "gemm workspace");
+    m->ws_rows = rows;
+  }
+  for (int64_t c0 = 0; c0 < b.n; c0 += m->ws_rows) {
+    const int64_t cnt = std::min<int64_t>(m->ws_rows, b.n - c0);
+    crs::Batch bc = b;
+    bc.n = cnt;
+    bc.T = b.T + c0;
+    bc.P = b.P + c0;
+    bc.Y = b.Y + c0;
+    bc.wdot = b.wdot + c0;
+    crs::mixed::QOut qo{m->d_ws, K, m->Kh, m->d_escale};
+    cudaError_t e = crs::launch_wdot_mixed_q(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s, qo);
+    if (e == cudaErrorNotSupported)
+      return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates kernel");
+    if (e != cudaSuccess) return cuda_fail(e, "gemm rates launch");
+    const int64_t M_pad = (cnt + 127) / 128 * 128;
+    e = crs::launch_gemm_wdot(m->d_ws, m->d_nuB, M_pad, m->N_pad, K, m->block_n, bc.wdot, b.ld,
+                              (int)cnt, m->L.N, m->d_escale, m->d_status, s);
+    if (e != cudaSuccess) return cuda_fail(e, "gemm contraction launch");
+  }
+  return CRS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -402,6 +494,9 @@ int crs_mech_free(crs_mech *m) {
   if (!m) return CRS_OK;
   if (m->d_img) cudaFree(m->d_img);
   if (m->d_status) cudaFree(m->d_status);
+  if (m->d_nuB) cudaFree(m->d_nuB);
+  if (m->d_ws) cudaFree(m->d_ws);
+  if (m->d_escale) cudaFree(m->d_escale);
   delete m;
   return CRS_OK;
 }
@@ -532,6 +627,14 @@ int crs_wdot_stages(const crs_mech *m, int64_t n, const double *T,
     case CRS_MODE_MIXED_WARP:
       e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
+    case CRS_MODE_GEMM: {
+      if (conc || fwd || rev || pres_mod)
+        return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_GEMM does not write intermediates");
+      int rc2 = wdot_gemm(const_cast<crs_mech *>(m), b, s);
+      if (rc2 != CRS_OK) return rc2;
+      e = cudaSuccess;
+      break;
+    }
     default:
       return fail(CRS_ERR_ARG, "unknown mode %d", mode);
   }

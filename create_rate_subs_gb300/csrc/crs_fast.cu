@@ -594,7 +594,7 @@ __global__ void __launch_bounds__(128, 1)
 // reaction order.  Per-state scalars (1/T, ln T) are computed once per
 // state by one lane of a 32-state batch.  With no per-thread arrays, many
 // more warps fit on an SM than with one state per thread.
-constexpr int DW = 8;  // warps per CTA
+constexpr int DW = 8;  // most warps per CTA
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -624,8 +624,9 @@ __global__ void __launch_bounds__(DW * 32)
   double *q = wb + 128 + 2 * N;
   const int l0 = t.lane_ptr[lane], l1 = t.lane_ptr[lane + 1];
   int bad = 0;
-  const int64_t nwarp = (int64_t)gridDim.x * DW;
-  for (int64_t i0 = ((int64_t)blockIdx.x * DW + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
+  const int nw = blockDim.x >> 5;
+  const int64_t nwarp = (int64_t)gridDim.x * nw;
+  for (int64_t i0 = ((int64_t)blockIdx.x * nw + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
     // per-state scalars of a batch of 32 consecutive states, one per lane
     {
       const int64_t i = i0 + lane;
@@ -723,29 +724,27 @@ cudaError_t launch_wdot_fp64(const unsigned char *img, const ImgLayout &L,
                              const Batch &b, int sm_count, int smem_optin,
                              cudaStream_t s) {
   const int per_warp = 128 + 2 * L.N + L.R + 1;  // doubles
-  const size_t warps = (size_t)fast::DW * per_warp * sizeof(double);
+  const size_t pw = (size_t)per_warp * sizeof(double);
   const size_t tab = (size_t)(L.rng[1][1] - L.rng[1][0] + L.rng[1][3] - L.rng[1][2]);
   const bool stages = b.conc || b.fwd || b.rev || b.pm;
-  const int threads = fast::DW * 32;
   const int64_t nbatch = (b.n + 31) / 32;
-  if (tab + warps <= (size_t)smem_optin) {
-    const size_t bytes = tab + warps;
-    auto k = stages ? fast::k_wdot_warp<true, true> : fast::k_wdot_warp<false, true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, bytes);
-    const int grid = grid_for(nbatch, fast::DW, sm_count * (per_sm > 0 ? per_sm : 1));
-    k<<<grid, threads, bytes, s>>>(img, L, b, per_warp);
-  } else if (warps <= (size_t)smem_optin) {
-    auto k = stages ? fast::k_wdot_warp<true, false> : fast::k_wdot_warp<false, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warps);
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, warps);
-    const int grid = grid_for(nbatch, fast::DW, sm_count * (per_sm > 0 ? per_sm : 1));
-    k<<<grid, threads, warps, s>>>(img, L, b, per_warp);
-  } else {
-    return cudaErrorNotSupported;
+  // tables on chip with 8 warps if they fit, else tables in global memory
+  // and as many warps (up to 8) as the per-warp buffers allow
+  bool smem_tab = tab + fast::DW * pw <= (size_t)smem_optin;
+  int nw = fast::DW;
+  if (!smem_tab) {
+    nw = (int)((size_t)smem_optin / pw);
+    if (nw > fast::DW) nw = fast::DW;
+    if (nw < 1) return cudaErrorNotSupported;
   }
+  const size_t bytes = (smem_tab ? tab : 0) + nw * pw;
+  auto k = smem_tab ? (stages ? fast::k_wdot_warp<true, true> : fast::k_wdot_warp<false, true>)
+                    : (stages ? fast::k_wdot_warp<true, false> : fast::k_wdot_warp<false, false>);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  const int grid = grid_for(nbatch, nw, sm_count * (per_sm > 0 ? per_sm : 1));
+  k<<<grid, nw * 32, bytes, s>>>(img, L, b, per_warp);
   return cudaGetLastError();
 }
 

@@ -219,6 +219,27 @@ struct EpiStoreF32 {
   }
 };
 
+// wdot[col * ld + row] += acc * 2^escale[row]: the contraction's epilogue
+// (column-major FP64 output: consecutive lanes write consecutive states).
+struct EpiWdot {
+  double *out;
+  int64_t ld;
+  int m_valid, n_valid;
+  const int *escale;
+  __device__ void operator()(int row, int col0, const uint32_t (&v)[32]) const {
+    if (row >= m_valid) return;
+    const double sc = __hiloint2double((escale[row] + 1023) << 20, 0);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int col = col0 + j;
+      if (col < n_valid) {
+        double *o = out + (int64_t)col * ld + row;
+        *o = fma((double)__uint_as_float(v[j]), sc, *o);
+      }
+    }
+  }
+};
+
 }  // namespace gemm
 
 // ---- host side ------------------------------------------------------------
@@ -272,6 +293,24 @@ cudaError_t launch_gemm(const CUtensorMap &ta, const CUtensorMap &tb, int64_t M_
   dim3 grid((unsigned)(M_pad / gemm::BM), (unsigned)(N_pad / BN));
   k<<<grid, 128, smem, s>>>(ta, tb, (int)(K / gemm::BK), epi, status);
   return cudaGetLastError();
+}
+
+// Contraction of a chunk: wdot[n][row] += sum_k A[row][k] * B[n][k] * 2^e[row].
+cudaError_t launch_gemm_wdot(const void *A, const void *B, int64_t M_pad, int64_t N_pad,
+                             int64_t K, int block_n, double *out, int64_t ld, int m_valid,
+                             int n_valid, const int *escale, int32_t *status,
+                             cudaStream_t s) {
+  CUtensorMap ta, tb;
+  if (!make_tmap_bf16(&ta, A, M_pad, K, gemm::BM) || !make_tmap_bf16(&tb, B, N_pad, K, block_n))
+    return cudaErrorInvalidValue;
+  gemm::EpiWdot epi{out, ld, m_valid, n_valid, escale};
+  switch (block_n) {
+    case 64: return launch_gemm<64>(ta, tb, M_pad, N_pad, K, epi, status, s);
+    case 128: return launch_gemm<128>(ta, tb, M_pad, N_pad, K, epi, status, s);
+    case 192: return launch_gemm<192>(ta, tb, M_pad, N_pad, K, epi, status, s);
+    case 256: return launch_gemm<256>(ta, tb, M_pad, N_pad, K, epi, status, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace crs

@@ -114,6 +114,18 @@ __host__ __device__ inline Tab make_tab(const unsigned char *b,
   return make_tab2(b, b, L, 0, 0);
 }
 
+namespace mixed {
+// Output of the mixed rates-only kernel that feeds the tensor-core
+// contraction: per state s a bf16 row A[s] = [hi(q_0..q_R-1), 0.., lo(...)]
+// of q * 2^-c_s (Kh columns each), c_s in escale[s].
+struct QOut {
+  void *A;        // __nv_bfloat16 rows
+  int64_t lda;    // 2 * Kh
+  int Kh;
+  int *escale;
+};
+}  // namespace mixed
+
 // A derived table computed on the host at load time.
 struct Derived {
   int ImgLayout::*field;

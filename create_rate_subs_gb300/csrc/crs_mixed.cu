@@ -26,6 +26,7 @@
 
 #include "crs_internal.cuh"
 #include "crs_shapes.cuh"
+#include <cuda_bf16.h>
 
 namespace crs {
 namespace mixed {
@@ -494,7 +495,7 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ---- warp per state (see crs_fast.cu for the layout) --------------------
-constexpr int DW = 8;
+constexpr int DW = 8;  // most warps per CTA
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -502,10 +503,19 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <bool STAGES, bool SMEM_TAB>
+// Rates-only variant (OUTQ, see QOut): terms whose binary exponent lies
+// more than WINDOW from the state's scale c_s are summed here in FP64
+// instead and written to wdot, to which the contraction then adds.
+constexpr int WINDOW = 100;
+
+__device__ __forceinline__ int dexp2(double v) {
+  return (int)((__double2hiint(v) >> 20) & 0x7ff) - 1023;
+}
+
+template <bool STAGES, bool SMEM_TAB, bool OUTQ>
 __global__ void __launch_bounds__(DW * 32)
     k_wdot_warp(const unsigned char *__restrict__ img, ImgLayout L, Batch b,
-                int per_warp) {
+                int per_warp, QOut qo) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   int nb = 0;
@@ -522,10 +532,12 @@ __global__ void __launch_bounds__(DW * 32)
   const DArr S{wb + 128};
   double *q = wb + 128 + N;
   const FArr C{reinterpret_cast<float *>(wb + 128 + N + R)};
+  uint32_t *mask = reinterpret_cast<uint32_t *>(wb + 128 + N + R + (N + 1) / 2);
   const int l0 = t.lane_ptr[lane], l1 = t.lane_ptr[lane + 1];
   int bad = 0;
-  const int64_t nwarp = (int64_t)gridDim.x * DW;
-  for (int64_t i0 = ((int64_t)blockIdx.x * DW + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
+  const int nw = blockDim.x >> 5;
+  const int64_t nwarp = (int64_t)gridDim.x * nw;
+  for (int64_t i0 = ((int64_t)blockIdx.x * nw + warp) * 32; i0 < b.n; i0 += nwarp * 32) {
     {
       const int64_t i = i0 + lane;
       const double T = i < b.n ? b.T[i] : 1000.0;
@@ -584,13 +596,56 @@ __global__ void __launch_bounds__(DW * 32)
         }
       }
       __syncwarp();
-      for (int a = l0; a < l1; ++a) {
-        const int k = t.lane_sp[a];
-        double w = 0.0;
-        for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e)
-          w = fma(t.spc_nu[e], q[t.spc_r[e]], w);  // FP64 accumulation
-        bad += !isfinite(w);
-        b.wdot[(int64_t)k * b.ld + i] = w;
+      if (!OUTQ) {
+        for (int a = l0; a < l1; ++a) {
+          const int k = t.lane_sp[a];
+          double w = 0.0;
+          for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e)
+            w = fma(t.spc_nu[e], q[t.spc_r[e]], w);  // FP64 accumulation
+          bad += !isfinite(w);
+          b.wdot[(int64_t)k * b.ld + i] = w;
+        }
+      } else {
+        // scale centre: mean binary exponent of the nonzero finite terms
+        int esum = 0, ecnt = 0;
+        for (int r = lane; r < R; r += 32) {
+          const double v = q[r];
+          if (v != 0.0 && isfinite(v)) {
+            esum += dexp2(v);
+            ++ecnt;
+          }
+        }
+        for (int w = lane; w < (R + 31) / 32; w += 32) mask[w] = 0u;
+        esum = __reduce_add_sync(0xffffffffu, esum);
+        ecnt = __reduce_add_sync(0xffffffffu, ecnt);
+        const int c = ecnt ? (int)lrint((double)esum / ecnt) : 0;
+        if (lane == 0) qo.escale[i] = c;
+        __syncwarp();
+        const double sc = __hiloint2double((-c + 1023) << 20, 0);  // 2^-c
+        __nv_bfloat16 *row = static_cast<__nv_bfloat16 *>(qo.A) + (int64_t)i * qo.lda;
+        for (int r = lane; r < qo.Kh; r += 32) {
+          double v = r < R ? q[r] : 0.0;
+          const bool inwin = v == 0.0 || (isfinite(v) && abs(dexp2(v) - c) <= WINDOW);
+          if (!inwin) {
+            atomicOr(&mask[r >> 5], 1u << (r & 31));
+            v = 0.0;
+          }
+          const float f = (float)(v * sc);
+          const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+          row[r] = hi;
+          row[qo.Kh + r] = __float2bfloat16_rn(f - __bfloat162float(hi));
+        }
+        __syncwarp();
+        // out-of-window terms in FP64, in reaction order per species
+        for (int a = l0; a < l1; ++a) {
+          const int k = t.lane_sp[a];
+          double w = 0.0;
+          for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e) {
+            const int r = t.spc_r[e];
+            if (mask[r >> 5] & (1u << (r & 31))) w = fma(t.spc_nu[e], q[r], w);
+          }
+          b.wdot[(int64_t)k * b.ld + i] = w;
+        }
       }
       __syncwarp();
     }
@@ -618,35 +673,44 @@ cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
   return cudaGetLastError();
 }
 
+// Warp-per-state mixed kernel.  qo.A == nullptr: full wdot (CSR sum in
+// FP64); else the rates-only variant for the tensor-core contraction.
+cudaError_t launch_wdot_mixed_q(const unsigned char *img, const ImgLayout &L,
+                                const Batch &b, int sm_count, int smem_optin,
+                                cudaStream_t s, const mixed::QOut &qo) {
+  // doubles: 4 x 32 scalars, S[N], q[R], C[N] floats, R-bit mask
+  const int per_warp = 128 + L.N + L.R + (L.N + 1) / 2 + (L.R + 63) / 64 + 1;
+  const size_t pw = (size_t)per_warp * sizeof(double);
+  const size_t tab = (size_t)(L.rng[3][1] - L.rng[3][0] + L.rng[3][3] - L.rng[3][2]);
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  const bool outq = qo.A != nullptr;
+  const int64_t nbatch = (b.n + 31) / 32;
+  bool smem_tab = tab + mixed::DW * pw <= (size_t)smem_optin;
+  int nw = mixed::DW;
+  if (!smem_tab) {
+    nw = (int)((size_t)smem_optin / pw);
+    if (nw > mixed::DW) nw = mixed::DW;
+    if (nw < 1) return cudaErrorNotSupported;
+  }
+  const size_t bytes = (smem_tab ? tab : 0) + nw * pw;
+  auto k = outq ? (smem_tab ? mixed::k_wdot_warp<false, true, true>
+                            : mixed::k_wdot_warp<false, false, true>)
+                : smem_tab ? (stages ? mixed::k_wdot_warp<true, true, false>
+                                     : mixed::k_wdot_warp<false, true, false>)
+                           : (stages ? mixed::k_wdot_warp<true, false, false>
+                                     : mixed::k_wdot_warp<false, false, false>);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  const int grid = grid_for(nbatch, nw, sm_count * (per_sm > 0 ? per_sm : 1));
+  k<<<grid, nw * 32, bytes, s>>>(img, L, b, per_warp, qo);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_wdot_mixed(const unsigned char *img, const ImgLayout &L,
                               const Batch &b, int sm_count, int smem_optin,
                               cudaStream_t s) {
-  // doubles: 4 x 32 scalars, S[N], q[R], then C[N] as floats
-  const int per_warp = 128 + L.N + L.R + (L.N + 1) / 2 + 1;
-  const size_t warps = (size_t)mixed::DW * per_warp * sizeof(double);
-  const size_t tab = (size_t)(L.rng[3][1] - L.rng[3][0] + L.rng[3][3] - L.rng[3][2]);
-  const bool stages = b.conc || b.fwd || b.rev || b.pm;
-  const int threads = mixed::DW * 32;
-  const int64_t nbatch = (b.n + 31) / 32;
-  if (tab + warps <= (size_t)smem_optin) {
-    const size_t bytes = tab + warps;
-    auto k = stages ? mixed::k_wdot_warp<true, true> : mixed::k_wdot_warp<false, true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, bytes);
-    const int grid = grid_for(nbatch, mixed::DW, sm_count * (per_sm > 0 ? per_sm : 1));
-    k<<<grid, threads, bytes, s>>>(img, L, b, per_warp);
-  } else if (warps <= (size_t)smem_optin) {
-    auto k = stages ? mixed::k_wdot_warp<true, false> : mixed::k_wdot_warp<false, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warps);
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, warps);
-    const int grid = grid_for(nbatch, mixed::DW, sm_count * (per_sm > 0 ? per_sm : 1));
-    k<<<grid, threads, warps, s>>>(img, L, b, per_warp);
-  } else {
-    return cudaErrorNotSupported;
-  }
-  return cudaGetLastError();
+  return launch_wdot_mixed_q(img, L, b, sm_count, smem_optin, s, mixed::QOut{});
 }
 
 }  // namespace crs

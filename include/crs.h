@@ -54,6 +54,13 @@ typedef struct crs_mech crs_mech;
 #define CRS_MODE_MIXED_TPS 4
 #define CRS_MODE_FP64_WARP 5
 #define CRS_MODE_MIXED_WARP 6
+/* Mixed-precision rates, then the stoichiometric contraction
+ * wdot = q . nu as a BF16 tensor-core GEMM (q split into bf16 hi + lo,
+ * scaled per state; terms far outside the scale summed in FP64; FP32
+ * accumulation).  For large mechanisms.  Uses a workspace owned by the
+ * handle (allocated on first use, <= 2^18 states x 4 x R_pad bytes);
+ * calls on one handle are serialised.  No intermediates. */
+#define CRS_MODE_GEMM 7
 
 /* ---- mechanism tables ------------------------------------------------ */
 

@@ -127,9 +127,15 @@ def _cc(args, cwd):
     return res.returncode, res.stdout + res.stderr
 
 
-def compile_ref(name, opt_parity="-O2", opt_fast="-O3"):
-    """Build libref.so (parity) and libref_omp.so (timed) for one name."""
+def compile_ref(name, opt_parity=None, opt_fast=None):
+    """Build libref.so (parity) and libref_omp.so (timed) for one name.
+
+    Straight-line files of several MB (thousands of reactions) compile with
+    -O1 / -O2 to keep the build within a minute or two."""
     d = ref_dir(name)
+    big = os.path.getsize(os.path.join(d, "rxn_rates.c")) > 1_000_000
+    opt_parity = opt_parity or ("-O1" if big else "-O2")
+    opt_fast = opt_fast or ("-O2" if big else "-O3")
     nsp, nr, nrev, npm = dims(name)
     srcs = ["chem_utils.c", "rxn_rates.c", "spec_rates.c"]
     if npm:

@@ -221,3 +221,55 @@ def test_argument_errors(synth_mech):
     rc = lib.crs_wdot(rs.h, 8, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(P.data_ptr()),
                       ctypes.c_void_p(Y.data_ptr()), 8, ctypes.c_void_p(w.data_ptr()), 99, None)
     assert rc == 1
+
+
+# ---- tensor-core contraction (CRS_MODE_GEMM) and large mechanisms --------
+
+TOL_WDOT_GEMM = 1e-4   # bf16 hi+lo terms (~2^-17 each) summed in fp32
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gemm_mode_vs_golden(case, golden):
+    mech, g = golden(case)
+    rs = _rs(mech)
+    T, P, Y = _dev(g["T"], g["P"], g["Y"])
+    w = rs.wdot(T, P, Y, "gemm").cpu().numpy()
+    G = gross_scale(mech.tables, g["fwd"], g["rev"], g["pm"])
+    err = wdot_errors(w, g["wdot"], G)
+    print(case, err)
+    assert err["scaled"] <= TOL_WDOT_GEMM, err
+    assert rs.status() == (0, 0)
+
+
+@pytest.mark.parametrize("n", [1, 127, 129, 5000, (1 << 18) + 77])
+def test_gemm_mode_sizes_and_chunks(n, synth_mech):
+    """Tails of the 128-row tiles and more states than one workspace chunk;
+    checked against the FP64 kernel (itself pinned to the oracle)."""
+    mech = synth_mech("gri53")
+    T, P, Y = synth.make_states(mech.n_species, n, seed=n + 1)
+    rs = _rs(mech)
+    dT, dP, dY = _dev(T, P, Y)
+    ref = rs.wdot_stages(dT, dP, dY, "fp64_strict")
+    w = rs.wdot(dT, dP, dY, "gemm").cpu().numpy()
+    R = {k: v.cpu().numpy() for k, v in ref.items()}
+    G = gross_scale(mech.tables, R["fwd"], R["rev"], R["pm"])
+    assert wdot_errors(w, R["wdot"], G)["scaled"] <= TOL_WDOT_GEMM
+
+
+def test_large_mechanism_all_modes(synth_mech):
+    """561 species / 2539 reactions: tables in global memory, warp-per-state
+    kernels, and the tensor-core contraction, against the oracle."""
+    mech = synth_mech("large561")
+    n = 600
+    T, P, Y = synth.make_states(mech.n_species, n, seed=21)
+    ref = Oracle(mech.blob).eval(T, P, Y)
+    G = gross_scale(mech.tables, ref["fwd"], ref["rev"], ref["pm"])
+    rs = _rs(mech)
+    dT, dP, dY = _dev(T, P, Y)
+    for mode, tol in (("fp64", TOL_WDOT_FP64), ("fp64_strict", TOL_WDOT_FP64),
+                      ("mixed", TOL_WDOT_MIXED), ("gemm", TOL_WDOT_GEMM)):
+        w = rs.wdot(dT, dP, dY, mode).cpu().numpy()
+        err = wdot_errors(w, ref["wdot"], G)
+        print("large561", mode, err)
+        assert err["scaled"] <= tol, (mode, err)
+    assert rs.status() == (0, 0)
