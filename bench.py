@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--states", type=int, default=N_STATES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--large-states", type=int, default=1 << 20)
+    ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one launch of each wdot kernel on 2^18 states (for ncu)")
     return ap.parse_args()
@@ -366,6 +368,9 @@ def run_ours(args):
         "status": {"flags": flags, "nonfinite": bad},
         "clocks": clocks,
     }
+    if not args.no_large:
+        del hT, hP, hY, hW
+        line["large_mechanism"] = _bench_large(args, stream, dist, world)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_sample(mech, n_target=n, seconds=12.0)
     if rank == 0:
@@ -373,6 +378,68 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def _bench_large(args, stream, dist, world):
+    """Large-mechanism configuration: 561 species / 2539 reactions, 2^20
+    states; CSR contraction on chip (fp64, mixed) vs the tensor-core
+    contraction (gemm); errors against fp64_strict on a sub-sample; the
+    contraction GEMM alone against the measured bf16 peak."""
+    import ctypes
+    import torch
+    from create_rate_subs_gb300 import _lib, synth
+    from create_rate_subs_gb300.mechanism import Mechanism
+    from create_rate_subs_gb300.rates import RateSubs
+    d = tempfile.mkdtemp(prefix="crs_bench_large_")
+    mp, tp = synth.write_mechanism("large561", d)
+    mech = Mechanism.from_chemkin(mp, tp)
+    rs = RateSubs(mech)
+    N = mech.n_species
+    n = args.large_states
+    T, P, Y = synth.make_states(N, n, seed=3000)
+    dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[: N - 1].copy()))
+    del Y
+    out = torch.empty((N, n), dtype=torch.float64, device="cuda")
+    res = {"mechanism": "synthetic large561: 561 species / 2539 reactions "
+                        "(254 three-body, 127 Troe, 156 irreversible)",
+           "n_states": n, "modes": {}}
+    sub = 4096
+    ref = rs.wdot_stages(dT[:sub], dP[:sub], dY[:, :sub], "fp64_strict")
+    for mode in ("fp64", "mixed", "gemm"):
+        ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), 2, 1, stream, dist)
+        w = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], mode)
+        res["modes"][mode] = {"value": n * world / (ms * 1e-3), "unit": "states/s",
+                              "ms_per_step": ms,
+                              "error_vs_fp64_strict": _scaled_error(mech.tables, w, ref)}
+    # the contraction GEMM alone, at one workspace chunk (2^18 states)
+    lib = _lib.load()
+    M, Kh = 1 << 18, (mech.n_reactions + 63) // 64 * 64
+    K, bn = 2 * Kh, 192
+    Np = (N + bn - 1) // bn * bn
+    A = torch.randn((M, K), device="cuda").to(torch.bfloat16)
+    B = torch.randint(-2, 3, (Np, K), device="cuda").to(torch.bfloat16)
+    D = torch.empty((M, Np), device="cuda", dtype=torch.float32)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    st = ctypes.c_void_p(stream.cuda_stream)
+    ms = _time_steps(lambda: _lib.check(lib.crs_gemm_bf16(p(A), p(B), p(D), M, Np, K, Np, bn,
+                                                          None, st)), 5, 2, stream, dist)
+    flops = 2.0 * M * N * (2 * mech.n_reactions)
+    peak = None
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    peak = peak or 1900.0
+    res["contraction_gemm"] = {
+        "shape": "M=%d states x N=%d species (padded %d) x K=2*%d (bf16 hi+lo, padded %d)"
+                 % (M, N, Np, mech.n_reactions, K),
+        "ms": ms, "achieved_tflops": flops / (ms * 1e-3) / 1e12, "peak_tflops": peak,
+        "frac": flops / (ms * 1e-3) / 1e12 / peak, "peak_note": "bf16 burst, of measured",
+        "flops_note": "algorithmic 2*M*N*K on the unpadded sizes"}
+    del A, B, D, out, dT, dP, dY
+    torch.cuda.empty_cache()
+    return res
 
 
 def _jsonable(o):
