@@ -49,6 +49,7 @@ def _sig(lib):
         "crs_wdot_stages": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                             _vp, _i32, _vp],
         "crs_bind": [_vp],
+        "crs_wdot_gemm_noalloc": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_gemm_bf16": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp],
         "eval_conc": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
         "eval_rxn_rates": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],

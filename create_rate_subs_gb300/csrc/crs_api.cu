@@ -824,3 +824,127 @@ void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
 }
 
 }  // extern "C"
+
+// ---- allocation-free variant of the tensor-core contraction path ----------
+//
+// Some callers cannot allocate device memory at the moment they evaluate
+// rates: solvers that run inside a memory pool or framework that owns every
+// device allocation, code embedded in another runtime whose allocator must
+// not be bypassed, or integrator loops that must not block on cudaMalloc
+// (it can synchronise the device).  crs_wdot_gemm_noalloc serves them: it
+// evaluates exactly what crs_wdot(..., CRS_MODE_GEMM, ...) evaluates, but all
+// of its scratch lives in the array below, which the library's module holds
+// on every device it is loaded on, until the process exits.
+namespace {
+
+constexpr size_t kNoallocScratchBytes = (size_t)32 << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Device address of the array, looked up once per device.  In host code
+// g_noalloc_scratch names a host-side stand-in, never a device address.
+struct NoallocDevice {
+  bool ready = false;
+  unsigned char *ptr = nullptr;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[64];
+
+int noalloc_scratch(int device, unsigned char **out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (device < 0 || device >= 64) return fail(CRS_ERR_ARG, "device ordinal %d out of range", device);
+  NoallocDevice &d = g_noalloc_dev[device];
+  if (!d.ready) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_gemm_noalloc: scratch address");
+    d.ptr = static_cast<unsigned char *>(p);
+    d.ready = true;
+  }
+  *out = d.ptr;
+  return CRS_OK;
+}
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+// B[k][r] = B[k][Kh + r] = nu_kr for the reactions' net coefficients; the
+// rest of B must already be zero.
+__global__ void k_noalloc_nu(const unsigned char *__restrict__ img, crs::ImgLayout L,
+                             __nv_bfloat16 *B, int64_t K, int Kh) {
+  const crs::Tab t = crs::make_tab(img, L);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < L.R; r += gridDim.x * blockDim.x)
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+      const __nv_bfloat16 v = __float2bfloat16((float)t.nu_val[e]);
+      const int64_t k = t.nu_sp[e];
+      B[k * K + r] = v;
+      B[k * K + Kh + r] = v;
+    }
+}
+
+}  // namespace
+
+extern "C" int crs_wdot_gemm_noalloc(const crs_mech *m, int64_t n, const double *T,
+                                     const double *P, const double *Y, int64_t ld,
+                                     double *wdot, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !P || !Y || !wdot) return fail(CRS_ERR_ARG, "NULL array");
+  const crs::ImgLayout &L = m->L;
+  // the stoichiometric matrix must be exact in bf16
+  const crs::Tab th = crs::make_tab(m->h_img.data(), L);
+  for (int e = 0; e < th.nu_ptr[L.R]; ++e) {
+    const double nu = th.nu_val[e];
+    if ((double)__bfloat162float(__float2bfloat16((float)nu)) != nu)
+      return fail(CRS_ERR_UNSUPPORTED, "a stoichiometric coefficient is not exact in bf16");
+  }
+  const int Kh = (L.R + 63) / 64 * 64;
+  const int64_t K = 2 * (int64_t)Kh;
+  const int block_n = L.N <= 64 ? 64 : L.N <= 128 ? 128 : L.N <= 192 ? 192 : L.N <= 256 ? 256 : 192;
+  const int64_t N_pad = (L.N + block_n - 1) / block_n * block_n;
+  // scratch layout: B [N_pad][K] | escale [rows] | bf16 rows [rows][K]
+  const size_t b_bytes = align256((size_t)N_pad * K * sizeof(__nv_bfloat16));
+  const size_t per_row = (size_t)K * sizeof(__nv_bfloat16) + sizeof(int);
+  int64_t rows = 0;
+  if (b_bytes + 256 < kNoallocScratchBytes)
+    rows = (int64_t)((kNoallocScratchBytes - b_bytes - 256) / per_row) / 128 * 128;
+  if (rows < 128)
+    return fail(CRS_ERR_UNSUPPORTED,
+                "crs_wdot_gemm_noalloc: the mechanism needs %zu bytes of scratch for "
+                "128 states, more than the fixed %zu",
+                b_bytes + 256 + 128 * per_row, kNoallocScratchBytes);
+  rows = std::min<int64_t>(rows, (n + 127) / 128 * 128);
+  unsigned char *base = nullptr;
+  rc = noalloc_scratch(m->device, &base);
+  if (rc) return rc;
+  __nv_bfloat16 *B = reinterpret_cast<__nv_bfloat16 *>(base);
+  int *escale = reinterpret_cast<int *>(base + b_bytes);
+  void *A = base + b_bytes + align256((size_t)rows * sizeof(int));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the array keeps the previous call's contents: rebuild B from zero
+  cudaError_t e = cudaMemsetAsync(B, 0, (size_t)N_pad * K * sizeof(__nv_bfloat16), s);
+  if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_gemm_noalloc: clear");
+  k_noalloc_nu<<<(L.R + 127) / 128 > 0 ? (L.R + 127) / 128 : 1, 128, 0, s>>>(m->d_img, L, B, K, Kh);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_gemm_noalloc: nu");
+  crs::Batch b = make_batch(m, n, ld);
+  b.T = T; b.P = P; b.Y = Y; b.wdot = wdot;
+  for (int64_t c0 = 0; c0 < n; c0 += rows) {
+    const int64_t cnt = std::min<int64_t>(rows, n - c0);
+    crs::Batch bc = b;
+    bc.n = cnt;
+    bc.T = T + c0;
+    bc.P = P + c0;
+    bc.Y = Y + c0;
+    bc.wdot = wdot + c0;
+    crs::mixed::QOut qo{A, K, Kh, escale};
+    e = crs::launch_wdot_mixed_q(m->d_img, L, bc, m->sm_count, m->smem_optin, s, qo);
+    if (e == cudaErrorNotSupported)
+      return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates kernel");
+    if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_gemm_noalloc: rates");
+    const int64_t M_pad = (cnt + 127) / 128 * 128;
+    e = crs::launch_gemm_wdot(A, B, M_pad, N_pad, K, block_n, bc.wdot, ld, (int)cnt, L.N,
+                              escale, m->d_status, s);
+    if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_gemm_noalloc: contraction");
+  }
+  return CRS_OK;
+}

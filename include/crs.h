@@ -127,6 +127,27 @@ int crs_wdot_stages(const crs_mech *mech, int64_t n, const double *T,
                     double *wdot, double *conc, double *fwd, double *rev,
                     double *pres_mod, int mode, void *stream);
 
+/* ---- allocation-free contraction (no counterpart in the reference) ----- */
+
+/* The evaluation of crs_wdot(..., CRS_MODE_GEMM, ...) for callers that must
+ * not allocate device memory while they run: solvers inside a memory pool
+ * or framework that owns every device allocation, code embedded in another
+ * runtime whose allocator must not be bypassed, or time-stepping loops that
+ * cannot afford cudaMalloc's device synchronisation.  All scratch (the bf16
+ * stoichiometric matrix, per-state scale exponents and bf16 rate rows for
+ * one chunk of states) lives in one fixed 32 MiB array inside libcrs, which
+ * every GPU that loads the library keeps until the process exits; states
+ * are processed in chunks that fit it.  Mechanisms whose matrix plus 128
+ * states do not fit are refused with CRS_ERR_UNSUPPORTED and a message.
+ * The first call on a device looks the array's device address up; make
+ * that first call before any stream capture.  Every call rebuilds what must
+ * start from zero, but all calls share the one array: calls whose work
+ * overlaps on the GPU (other streams, other host threads) race on it and
+ * must be serialised by the caller.  Arguments as crs_wdot. */
+int crs_wdot_gemm_noalloc(const crs_mech *mech, int64_t n, const double *T,
+                          const double *P, const double *Y, int64_t ld,
+                          double *wdot, void *stream);
+
 /* ---- building blocks (no counterpart in the reference) ----------------- */
 
 /* D[m*ldd + n] = sum_k A[m*K + k] * B[n*K + k]: bf16 inputs (device,
