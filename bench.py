@@ -49,6 +49,13 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-states", type=int, default=1 << 20)
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--sur-train", type=int, default=1 << 24,
+                    help="surrogate training states")
+    ap.add_argument("--sur-epochs", type=int, default=8)
+    ap.add_argument("--sur-eval", type=int, default=1 << 24,
+                    help="fresh states the surrogate is evaluated on")
+    ap.add_argument("--sur-tol", type=float, default=0.05)
+    ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one launch of each wdot kernel on 2^18 states (for ncu)")
     return ap.parse_args()
@@ -368,8 +375,13 @@ def run_ours(args):
         "status": {"flags": flags, "nonfinite": bad},
         "clocks": clocks,
     }
+    del hT, hP, hY, hW
+    if not args.no_surrogate:
+        del dT, dP, dY, out
+        torch.cuda.empty_cache()
+        line["surrogate"] = _bench_surrogate(args, rs, stream, dist, world, rank)
+        torch.cuda.empty_cache()
     if not args.no_large:
-        del hT, hP, hY, hW
         line["large_mechanism"] = _bench_large(args, stream, dist, world)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_sample(mech, n_target=n, seconds=12.0)
@@ -378,6 +390,115 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def _bench_surrogate(args, rs, stream, dist, world, rank):
+    """The learned surrogate on the 53-species mechanism: trained by the
+    library's own bf16 kernels on states labelled by the exact FP64 kernel,
+    evaluated with fallback on fresh states; error against the exact FP64
+    kernel on every evaluated state."""
+    import torch
+    from create_rate_subs_gb300.surrogate import Surrogate
+    N = rs.n_species
+    B = 16384
+    sur = Surrogate(rs, seed=0, batch=B)
+    n_tr = (args.sur_train + B - 1) // B * B
+    T, P, Y = sur.sample_states(n_tr, seed=5000 + rank)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    losses = sur.fit(states=(T, P, Y), epochs=args.sur_epochs, lr=2e-3, lr_final=2e-5)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fit_s = e0.elapsed_time(e1) * 1e-3
+    del T, P, Y
+    torch.cuda.empty_cache()
+    net = sur.net
+    macs = sum(net.dims[l] * net.dims[l + 1] for l in range(net.L))
+    bwd_data = sum(net.dims[l] * net.dims[l + 1] for l in range(1, net.L))
+    train_flops_state = 2 * (2 * macs + bwd_data)
+    # a timed training pass alone (steps after the fit, same buffers)
+    nb = 64
+    Xb = torch.randn((B, net.pad[0]), device="cuda").to(torch.bfloat16)
+    XTb = Xb.t().contiguous()
+    Tgb = torch.randn((B, N), device="cuda")
+    Wsave = net.state_dict()
+    ms_step = _time_steps(lambda: net.train_step(Xb, XTb, Tgb, 1e-9), nb, 3, stream, dist)
+    net.load_state_dict(Wsave)
+    # evaluation on fresh states
+    ne = args.sur_eval
+    Te, Pe, Ye = sur.sample_states(ne, seed=7000 + rank)
+    Ye = Ye[: N - 1].contiguous()
+    out = torch.empty((N, ne), dtype=torch.float64, device="cuda")
+    exact = torch.empty((N, ne), dtype=torch.float64, device="cuda")
+    tol = args.sur_tol
+    ms_sur = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tol, out=out), 3, 1, stream, dist)
+    ms_net = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tol, out=out, with_fallback=False),
+                         3, 1, stream, dist)
+    ms_plain = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "fp64", out=exact), 3, 1, stream, dist)
+    ms_mixed = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "mixed", out=exact), 3, 1, stream, dist)
+    # the network's layers alone (features already in X)
+    M = (ne + 127) // 128 * 128
+    X = torch.zeros((M, net.pad[0]), dtype=torch.bfloat16, device="cuda")
+    sur.features(Te, Pe, Ye, ne, ne, X, box=False)
+    Yh = torch.empty((ne, net.pad[-1]), dtype=torch.float32, device="cuda")
+    ms_fwd = _time_steps(lambda: net.forward(X, ne, Yh), 5, 2, stream, dist)
+    del X, Yh
+    # error of the gated result and of the raw network, on every state
+    rs.wdot(Te, Pe, Ye, "fp64", out=exact)
+    w, nfb = sur.wdot(Te, Pe, Ye, tol=tol, out=out)
+    raw = torch.empty_like(out)
+    sur.wdot(Te, Pe, Ye, tol=tol, out=raw, with_fallback=False)
+    den = exact.abs() + sur.scale[:, None]
+
+    def q(e):
+        if e.numel() == 0:
+            return None
+        k = torch.sort(e.float()).values
+        n_ = k.numel()
+        return {"p50": float(k[n_ // 2]), "p90": float(k[int(n_ * 0.9)]),
+                "p99": float(k[int(n_ * 0.99)]), "max": float(k[-1])}
+    err_gated = q(((w - exact).abs() / den).amax(dim=0))
+    e_raw = ((raw - exact).abs() / den).amax(dim=0)
+    err_raw = q(e_raw)
+    served = (w == raw).all(dim=0)          # states the network answered
+    err_served = q(e_raw[served])
+    peak = None
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    peak = peak or 1900.0
+    fwd_tflops = 2.0 * macs * ne / (ms_fwd * 1e-3) / 1e12
+    res = {
+        "network": "MLP %s, SiLU, bf16 weights / fp32 accumulation, tcgen05 GEMMs"
+                   % "->".join(str(d) for d in net.dims),
+        "train_states": n_tr, "epochs": args.sur_epochs, "batch": B,
+        "train_loss_per_epoch": losses, "fit_seconds": fit_s,
+        "train_step_ms": ms_step,
+        "train_states_per_s": B * world / (ms_step * 1e-3),
+        "train_tflops": train_flops_state * B / (ms_step * 1e-3) / 1e12,
+        "eval_states": ne, "tol": tol,
+        "value": ne * world / (ms_sur * 1e-3), "unit": "states/s",
+        "ms_per_step": ms_sur,
+        "network_only_states_per_s": ne * world / (ms_net * 1e-3),
+        "plain_fp64_states_per_s": ne * world / (ms_plain * 1e-3),
+        "mixed_states_per_s": ne * world / (ms_mixed * 1e-3),
+        "speedup_vs_plain": ms_plain / ms_sur,
+        "fallback_fraction": nfb / ne,
+        "error_definition": "per state max_k |w_k - w_k,fp64| / (|w_k,fp64| + s_k), "
+                            "s_k = std of wdot_k over the training states",
+        "error_gated": err_gated, "error_network_all_states": err_raw,
+        "error_network_served_states": err_served,
+        "roofline": {"bound": "tensor", "kernel": "network forward (4 tcgen05 GEMMs + "
+                     "epilogues)", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": fwd_tflops / peak, "flops_per_state": 2 * macs,
+                     "peak_note": "bf16 burst, of measured"},
+    }
+    del Te, Pe, Ye, out, exact, w, raw, den, e_raw, served
+    return res
 
 
 def _bench_large(args, stream, dist, world):

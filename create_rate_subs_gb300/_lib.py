@@ -51,6 +51,24 @@ def _sig(lib):
         "crs_bind": [_vp],
         "crs_wdot_gemm_noalloc": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_gemm_bf16": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp],
+        "crs_mlp_forward": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _i32, _vp, _i64,
+                            _vp, _i64, _vp, _i64, _vp, _i64, _vp],
+        "crs_mlp_backward_data": [_vp, _vp, _i64, _i64, _i64, _i64, _i64, _vp, _i64, _vp,
+                                  _i64, _vp, _i64, _vp],
+        "crs_mlp_backward_weight": [_vp, _vp, _i64, _i64, _i64, _i64, _i64, _i32, _vp, _vp,
+                                    _vp],
+        "crs_mlp_row_sums": [_vp, _i64, _i64, _i64, _vp, _vp],
+        "crs_mlp_loss_grad": [_vp, _i64, _vp, _i64, _i64, _i64, _i64, ctypes.c_float, _vp,
+                              _i64, _vp, _i64, _vp, _vp],
+        "crs_adam_step": [_vp, _vp, _vp, _vp, _i64, _i64, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, ctypes.c_float, _i32, _vp, _i64, _vp, _i64, _vp],
+        "crs_surrogate_features": [_i64, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp,
+                                   _i64, _vp, _i64, _i32, _vp, _vp, _vp],
+        "crs_surrogate_output": [_i64, _vp, _i64, _i32, _vp, _vp, _vp, _i32, ctypes.c_float,
+                                 _vp, _vp, _i64, _vp, _vp],
+        "crs_select": [_i64, _vp, _vp, _vp, _vp],
+        "crs_gather_states": [_i64, _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp],
+        "crs_scatter_wdot": [_i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp],
         "eval_conc": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
         "eval_rxn_rates": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
         "get_rxn_pres_mod": [ctypes.c_double, ctypes.c_double, _vp, _vp],

@@ -86,6 +86,13 @@ int cuda_fail(cudaError_t e, const char *what) {
   return fail(CRS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+}  // namespace
+
+// Message for crs_last_error() from the other translation units.
+int crs::report(int code, const char *msg) { return fail(code, "%s", msg); }
+
+namespace {
+
 struct Section {
   uint32_t dtype;
   uint64_t count, offset;

@@ -224,4 +224,7 @@ __device__ inline bool stage_ranges(unsigned char *smem,
 
 #endif
 
+// Sets the text returned by crs_last_error() and returns code.
+int report(int code, const char *msg);
+
 }  // namespace crs

@@ -190,33 +190,32 @@ __device__ __forceinline__ ff rate_exponent(const Tab &t, int row,
 }
 
 // product of concentration factors as mantissa * 2^E
+// Product of concentration factors, times the mantissa m0 of the rate
+// constant, as mantissa * 2^E; the FP32 rounding of every multiply is kept
+// (FMA error terms) and added back once at the end.
 template <class FC>
-__device__ __forceinline__ float product(const int32_t *sp, const int32_t *nint,
-                                         const double *nu, int a, int b,
-                                         const FC &C, int &E) {
-  float m = 1.0f;
+__device__ __forceinline__ float product(float m0, const int32_t *sp,
+                                         const int32_t *nint, const double *nu,
+                                         int a, int b, const FC &C, int &E) {
+  float m = m0, err = 0.0f;
   for (int j = a; j < b; ++j) {
     const float c = C[sp[j]];
     int n = nint[j];
-    if (n < 0) {
-      int e;
-      const float f = fsplit(powf(c, (float)nu[j]), e);
-      m *= f;
-      E += e;
-      continue;
-    }
     int e;
-    const float f = fsplit(c, e);
+    const float f = fsplit(n < 0 ? powf(c, (float)nu[j]) : c, e);
+    if (n < 0) n = 1;
     for (; n > 0; --n) {
-      m *= f;
-      E += e;
-      // keep the mantissa product inside [2^-8, 2^8]
+      const float mm = m * f;
+      err = fmaf(err, f, fmaf(m, f, -mm));
+      // keep the mantissa inside [2^-8, 2^8]: rescale by a power of two
       int e2;
-      m = fsplit(m, e2);
-      E += e2;
+      const float ms = fsplit(mm, e2);
+      err = ldexpf(err, -e2);
+      m = ms;
+      E += e + e2;
     }
   }
-  return m;
+  return m + err;
 }
 
 // pres_mod entry p in FP32.  The reduced pressure enters through
@@ -276,7 +275,8 @@ __device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
     const float lF = log10f(fmaxf(f, 1.0e-37f));
     const float A = lP - 0.67f * lF - 0.4f;
     const float B = 0.806f - 1.1762f * lF - 0.14f * lP;
-    F = expf(LN10_F * lF / (1.0f + A * A / (B * B)));
+    const float B2 = B * B;
+    F = expf(LN10_F * lF * (B2 / fmaf(A, A, B2)));
   } else {
     const float *c = t.sri_ff + 8 * p;  // a, -b (ff), -1/c (ff), d, e
     const float X = 1.0f / (1.0f + lP * lP);
@@ -302,14 +302,17 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
     float sg;
     x[u] = rate_exponent(t, r, s, sg);
     int E;
-    float m = ff_exp(x[u], E);
+    float m = ff_exp(x[u], E), err = 0.0f;
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
       int e;
-      m *= fsplit(C[t.rfac[MAXF * r + q]], e);
+      const float f = fsplit(C[t.rfac[MAXF * r + q]], e);
+      const float mm = m * f;  // exact rounding error kept in err
+      err = fmaf(err, f, fmaf(m, f, -mm));
+      m = mm;
       E += e;
     }
-    fwd[u] = assemble(m, E);
+    fwd[u] = assemble(m + err, E);
     rev[u] = 0.0;
   }
   if (REV) {
@@ -321,14 +324,17 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
 #pragma unroll
       for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], S[t.nu_sp[e0 + q]], g);
       int E;
-      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double(g))), E);
+      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double(g))), E), err = 0.0f;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         int e;
-        m *= fsplit(C[t.pfac[MAXF * r + q]], e);
+        const float f = fsplit(C[t.pfac[MAXF * r + q]], e);
+        const float mm = m * f;
+        err = fmaf(err, f, fmaf(m, f, -mm));
+        m = mm;
         E += e;
       }
-      rev[u] = assemble(m, E);
+      rev[u] = assemble(m + err, E);
     }
   }
 #pragma unroll
@@ -384,8 +390,8 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   const ff xf = rate_exponent(t, r, s, sgn);
   int Ef;
   const float pf = ff_exp(xf, Ef);
-  const float mf = sgn * pf * product(t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
-                                      t.rx_ptr[r + 1], C, Ef);
+  const float mf = sgn * product(pf, t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
+                                 t.rx_ptr[r + 1], C, Ef);
   fwd = assemble(mf, Ef);
   const int j = t.rev_idx[r];
   double net = fwd;
@@ -396,8 +402,8 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
       g = fma(t.nu_val[e], S[t.nu_sp[e]], g);
     int Er;
     const float pr = ff_exp(ff_add(xf, ff_neg(ff_from_double(g))), Er);
-    const float mr = sgn * pr * product(t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r],
-                                        t.px_ptr[r + 1], C, Er);
+    const float mr = sgn * product(pr, t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r],
+                                   t.px_ptr[r + 1], C, Er);
     rev = assemble(mr, Er);
     net = fwd - rev;  // FP64
   }

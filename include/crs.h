@@ -159,6 +159,97 @@ int crs_gemm_bf16(const void *A, const void *B, float *D, int64_t M, int64_t N,
                   int64_t K, int64_t ldd, int block_n, int32_t *status,
                   void *stream);
 
+/* ---- surrogate network (no counterpart in the reference) -------------- */
+
+/* A BF16 multilayer perceptron for wdot(T, ln P, ln Y), trained and run on
+ * the tensor cores.  Matrices are device, row-major, bf16 unless stated;
+ * "pad" sizes are the allocated extents (zero-filled by the caller), the
+ * unpadded sizes say which outputs are written.  M (states) pads to 128,
+ * K to 64, layer widths to 64 (and to 128 where they are GEMM rows). */
+#define CRS_ACT_NONE 0
+#define CRS_ACT_SILU 1
+
+/* Z = X[M_pad][K] W[N_pad][K]^T + b; A = act(Z).  Each output may be NULL:
+ * Z fp32 [M][ldz] (kept for the backward pass), A bf16 [M][lda] (next
+ * layer's input), AT bf16 [N][ldat] (A transposed, for the weight
+ * gradient), Y32 fp32 [M][ldy] (the network's output layer). */
+int crs_mlp_forward(const void *X, const void *W, const float *b,
+                    int64_t M_pad, int64_t N_pad, int64_t K, int64_t M,
+                    int64_t N, int act, float *Z, int64_t ldz, void *A,
+                    int64_t lda, void *AT, int64_t ldat, float *Y32,
+                    int64_t ldy, void *stream);
+/* dZprev = (dZ[M_pad][Kout] WT[Nin_pad][Kout]^T) * silu'(Zprev): the
+ * gradient through a layer's weights and the previous SiLU; written
+ * row-major [M][ld] and transposed [Nin][ldt] (dZprevT may be NULL). */
+int crs_mlp_backward_data(const void *dZ, const void *WT, int64_t M_pad,
+                          int64_t Nin_pad, int64_t Kout, int64_t M,
+                          int64_t Nin, const float *Zprev, int64_t ldz,
+                          void *dZprev, int64_t ld, void *dZprevT,
+                          int64_t ldt, void *stream);
+/* dW[Nout][Nin] (fp32, dense) = dZT[Nout_pad][M_pad] AT[Nin_pad][M_pad]^T,
+ * the batch split into `splits` slices whose fp32 partial products
+ * (partial: splits * Nout_pad * Nin_pad floats) are summed in slice order.
+ * Nout_pad a multiple of 128; M_pad / 64 a multiple of splits. */
+int crs_mlp_backward_weight(const void *dZT, const void *AT, int64_t Nout_pad,
+                            int64_t Nin_pad, int64_t M_pad, int64_t Nout,
+                            int64_t Nin, int splits, float *partial,
+                            float *dW, void *stream);
+/* out[r] = sum_{i<m} X[r*ld + i] (fp32; the bias gradient from dZT). */
+int crs_mlp_row_sums(const void *X, int64_t ld, int64_t rows, int64_t m,
+                     float *out, void *stream);
+/* loss += scale * sum (Yh - Tg)^2 over [m][n]; dY = 2 scale (Yh - Tg) as
+ * bf16 [m][ld] and transposed [n_pad][ldtt] (columns n..n_pad zero). */
+int crs_mlp_loss_grad(const float *Yh, int64_t ldy, const float *Tg,
+                      int64_t ldt, int64_t m, int64_t n, int64_t n_pad,
+                      float scale, void *dY, int64_t ld, void *dYT,
+                      int64_t ldtt, float *loss, void *stream);
+/* Adam on fp32 master weights p[rows][cols] (moments m, v), bias-corrected
+ * for `step` (1-based); refreshes the bf16 copies W [rows][ldw] and
+ * WT [cols][ldwt] when not NULL. */
+int crs_adam_step(float *p, const float *g, float *m, float *v, int64_t rows,
+                  int64_t cols, float lr, float b1, float b2, float eps,
+                  int step, void *W, int64_t ldw, void *WT, int64_t ldwt,
+                  void *stream);
+/* Network input of n states (SoA as crs_wdot): features T, ln P and
+ * ln(Y_k + 1e-12) for all nsp species (Y_N = 1 - sum), standardised by
+ * mu/sd, as bf16 X [n][ldx] (zero to nfeat_pad; nfeat_pad and ldx
+ * multiples of 8, X 16-byte aligned) and XT [nfeat_pad][ldxt]
+ * (may be NULL).  out_of_box[i] = 1 when a raw feature is outside
+ * [lo, hi] (lo/hi/out_of_box may be NULL); raw (may be NULL) receives the
+ * unstandardised features [n][2 + nsp]. */
+int crs_surrogate_features(int64_t n, const double *T, const double *P,
+                           const double *Y, int64_t ld, int nsp,
+                           const float *mu, const float *sd, const float *lo,
+                           const float *hi, void *X, int64_t ldx, void *XT,
+                           int64_t ldxt, int nfeat_pad,
+                           unsigned char *out_of_box, float *raw,
+                           void *stream);
+/* wdot[k][i] = s_k sign(y) expm1(|y|) in FP64 from the network output
+ * Yh[i][k], the species scale given as s_k = scale_m[k] * 2^scale_e[k]
+ * (fp32 mantissa, int exponent: scales exceed the fp32 range).
+ * fallback[i] = 1 when out_of_box[i] or the element residual
+ * max_e |sum_k a_ek w_k| / sum_k a_ek (|w_k| + s_k) exceeds tol; cons
+ * [nelem][nsp] (nelem <= 8) = a_ek s_k / max_j a_ej s_j, a_ek the atoms
+ * of element e in species k. */
+int crs_surrogate_output(int64_t n, const float *Yh, int64_t ldy, int nsp,
+                         const float *scale_m, const int *scale_e,
+                         const float *cons, int nelem, float tol,
+                         const unsigned char *out_of_box, double *wdot,
+                         int64_t ld, unsigned char *fallback, void *stream);
+/* idx[0..count) = the i < n with flag[i] != 0, in no particular order
+ * (count: device int64, set by the call). */
+int crs_select(int64_t n, const unsigned char *flag, int64_t *idx,
+               int64_t *count, void *stream);
+/* Copy the m states idx[j] into compact SoA arrays (rows = species rows of
+ * Y), and compact wdot rows back to their places. */
+int crs_gather_states(int64_t m, const int64_t *idx, const double *T,
+                      const double *P, const double *Y, int64_t ld, int rows,
+                      double *Tc, double *Pc, double *Yc, int64_t ldc,
+                      void *stream);
+int crs_scatter_wdot(int64_t m, const int64_t *idx, const double *Wc,
+                     int64_t ldc, int rows, double *W, int64_t ld,
+                     void *stream);
+
 /* ---- measurement helper (no counterpart in the reference) ------------- */
 
 /* Issue-rate probes of the current device, operations per second:
