@@ -245,6 +245,8 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   std::vector<crs::Derived> derived;
   if (!crs::build_fast_tables(img, L, derived))
     return fail(CRS_ERR_BLOB, "could not derive fast tables");
+  L.kc_single = 1;
+  for (int j = 0; j < L.NREV; ++j) L.kc_single &= (t.kc_ptr[j + 1] - t.kc_ptr[j]) <= 1;
   using M = int crs::ImgLayout::*;
   std::vector<std::pair<M, std::vector<unsigned char>>> secs;
   auto raw = [&](M f, const char *name) {
@@ -260,7 +262,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       if (d.field == f) secs.emplace_back(f, d.bytes);
   };
   using IL = crs::ImgLayout;
-  // Region order T F S M D (see ImgLayout::rng):
+  // Region order T F S M K D (see ImgLayout::rng):
   // [T] one-state-per-thread tables
   der(&IL::perm); der(&IL::seg); der(&IL::rfac); der(&IL::pfac);
   const size_t iF = secs.size();
@@ -279,6 +281,11 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   const size_t iM = secs.size();
   // [M] mixed only
   der(&IL::rate_ff); der(&IL::inv_mw_f);
+  const size_t iK = secs.size();
+  // [K] per-reaction Kc polynomials (mixed, one state per thread)
+  der(&IL::kc_poly);
+  raw(&IL::kc_ptr, "kc_ptr"); raw(&IL::kc_tmid, "kc_tmid");
+  raw(&IL::kc_lo, "kc_lo"); raw(&IL::kc_hi, "kc_hi");
   const size_t iD = secs.size();
   // [D] one-state-per-warp tables
   der(&IL::dperm); der(&IL::spc_ptr); der(&IL::spc_r); der(&IL::spc_nu);
@@ -296,9 +303,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   der(&IL::eff_f);
   raw(&IL::rate_par, "rate_par"); raw(&IL::kc_pref, "kc_pref");
   raw(&IL::pm_troe, "pm_troe"); raw(&IL::pm_sri, "pm_sri");
-  raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::kc_ptr, "kc_ptr");
-  raw(&IL::kc_tmid, "kc_tmid"); raw(&IL::kc_lo, "kc_lo");
-  raw(&IL::kc_hi, "kc_hi"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
+  raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
   // every blob section and every derived table must have been placed
   for (auto &w : want) {
     bool found = false;
@@ -324,11 +329,12 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   L2.bytes = (int)out.size();
   starts.push_back((int)out.size());
   const int T0 = starts[0], F0 = starts[iF], S0 = starts[iS], M0 = starts[iM],
-            D0 = starts[iD], C0 = starts[iC];
-  const int rng[4][4] = {{T0, M0, 0, 0},    // FP64 per thread: T F S
+            K0 = starts[iK], D0 = starts[iD], C0 = starts[iC];
+  const int rng[5][4] = {{T0, M0, 0, 0},    // FP64 per thread: T F S
                          {F0, M0, D0, C0},  // FP64 per warp: F S + D
-                         {T0, F0, S0, D0},  // mixed per thread: T + S M
-                         {S0, C0, 0, 0}};   // mixed per warp: S M D
+                         {T0, F0, S0, K0},  // mixed per thread: T + S M
+                         {S0, K0, D0, C0},  // mixed per warp: S M + D
+                         {T0, F0, S0, D0}}; // mixed per thread: T + S M K
   memcpy(L2.rng, rng, sizeof rng);
   img.swap(out);
   L = L2;
@@ -618,9 +624,10 @@ int crs_wdot_stages(const crs_mech *m, int64_t n, const double *T,
         e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_MIXED:
-      e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      // one state per thread when its columns fit on chip, else per warp
+      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       if (e == cudaErrorNotSupported)
-        e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+        e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_FP64_TPS:
       e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);

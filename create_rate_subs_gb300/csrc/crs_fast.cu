@@ -89,6 +89,27 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   for (int j = 0; j < 256; ++j) et[j] = (double)exp2l((long double)j / 256.0L);
   put(extra, &ImgLayout::rate_x, rx);
   put(extra, &ImgLayout::kc_lpref, lp);
+  // Kc polynomials with the prefactor folded in (single T_common group)
+  bool single = true;
+  for (int j = 0; j < L.NREV; ++j) single &= (t.kc_ptr[j + 1] - t.kc_ptr[j]) <= 1;
+  std::vector<double> kp(16 * (size_t)(single && L.NREV > 0 ? L.NREV : 1), 0.0);
+  if (single) {
+    for (int j = 0; j < L.NREV; ++j) {
+      double *o = kp.data() + 16 * j;
+      o[0] = INFINITY;  // no group: the zero polynomial on both sides
+      if (t.kc_ptr[j + 1] > t.kc_ptr[j]) {
+        const int g = t.kc_ptr[j];
+        o[0] = t.kc_tmid[g];
+        for (int c = 0; c < 7; ++c) {
+          o[2 + c] = t.kc_lo[7 * g + c];
+          o[9 + c] = t.kc_hi[7 * g + c];
+        }
+      }
+      o[2] += lp[j];
+      o[9] += lp[j];
+    }
+  }
+  put(extra, &ImgLayout::kc_poly, kp);
   put(extra, &ImgLayout::troe_x, tx);
   put(extra, &ImgLayout::sri_x, sx);
   put(extra, &ImgLayout::sp_gibbs, g);

@@ -27,8 +27,10 @@ struct ImgLayout {
   // shared memory (two ranges per kernel, copied back to back); sections
   // outside them are read from global memory through L1.
   //   [0] FP64 one state per thread   [1] FP64 one state per warp
-  //   [2] mixed one state per thread  [3] mixed one state per warp
-  int rng[4][4];
+  //   [2] mixed one state per thread, Kc polynomials read through L1
+  //   [3] mixed one state per warp
+  //   [4] mixed one state per thread, Kc polynomials in shared memory
+  int rng[5][4];
   // derived f64 sections (fast kernels): per rate row (logA, b, -Ta); per
   // reversible reaction log(Kc prefactor); per pres_mod entry the Troe and
   // SRI constants in multiply form; per species the 2x7 Gibbs
@@ -38,6 +40,11 @@ struct ImgLayout {
   // float-float pairs and sign(A); 1/mw; Troe and SRI constants (exponent
   // factors as float-float pairs); efficiencies minus one.
   int rate_ff, inv_mw_f, troe_ff, sri_ff, eff_f;
+  // derived f64 section (mixed, one state per thread): per reversible
+  // reaction 16 doubles [T_common, 0, lo c0..c6, hi c0..c6] of its Kc
+  // exponent polynomial with ln(prefactor) folded into c0; built when every
+  // reaction has a single T_common group (kc_single = 1)
+  int kc_poly, kc_single;
   // derived i32 sections: reaction processing order, start of each shape
   // group in it (crs_shapes.cuh), expanded reactant / product factors
   int perm, seg, rfac, pfac;
@@ -60,7 +67,8 @@ struct Tab {
   const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
   const double *spc_nu;
   const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
-  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab;
+  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly;
+  int kc_single;
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
       *sp_hi, *kc_dnu;
@@ -87,7 +95,7 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
 #define CRS_S(x) t.x = reinterpret_cast<const float *>(CRS_P(x))
 #define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
   CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
-  CRS_F(exptab);
+  CRS_F(exptab); CRS_F(kc_poly);
   CRS_I(perm); CRS_I(seg); CRS_I(rfac); CRS_I(pfac);
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
@@ -106,6 +114,7 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
 #undef CRS_S
 #undef CRS_I
   t.N = L.N; t.R = L.R; t.NREV = L.NREV; t.NPM = L.NPM;
+  t.kc_single = L.kc_single;
   return t;
 }
 
@@ -204,7 +213,14 @@ __device__ inline bool stage_to_smem(void *sdst, const void *gsrc, int bytes,
   }
   // every thread must agree before anyone leaves
   int all = __syncthreads_and(done ? 1 : 0);
-  if (!all && threadIdx.x == 0 && status) atomicOr(&status[0], STATUS_STAGE_TIMEOUT);
+  if (!all) {
+    // give up, but not while the copies may still be writing this CTA's
+    // shared memory: wait for them once more (bounded, 16x longer)
+    if (threadIdx.x == 0 && status) atomicOr(&status[0], STATUS_STAGE_TIMEOUT);
+    for (int it = 0; it < (1 << 26); ++it)
+      if (mbar_try_wait(b, 0)) break;
+    __syncthreads();
+  }
   return all != 0;
 }
 

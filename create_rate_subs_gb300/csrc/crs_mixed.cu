@@ -23,6 +23,7 @@
 // measured by the tests and reported by bench.py.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <type_traits>
 
 #include "crs_internal.cuh"
 #include "crs_shapes.cuh"
@@ -90,44 +91,68 @@ __device__ __forceinline__ ff ff_from_double(double d) {
   return ff{h, d2f_rn(d - f2d_exact(h))};
 }
 
-// value m * 2^E as a double, by integer operations; m is an FP32 number
-// whose magnitude stays within [2^-8, 2^8] or is zero / non-finite
+// The same split by integer operations only (no FP64 instruction): h = d
+// truncated to 24 significant bits, l = the remaining 29 bits of the
+// significand converted once to fp32.  |d| below 2^-100 gives (0, 0), an
+// absolute error far below what an exponent argument can notice.
+__device__ __forceinline__ ff ff_from_double_int(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  if (e < -100 || e > 127) return e > 127 ? ff{d2f_rn(d), 0.0f} : ff{0.0f, 0.0f};
+  const unsigned sign = hi & 0x80000000u;
+  const float h = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | ((hi & 0xfffffu) << 3) |
+                                  (lo >> 29));
+  const float m = (float)(lo & 0x1fffffffu);  // exact below 2^24, else rounded once
+  // times 2^(e - 52): one normal power of two for e >= -74, else two
+  const float l = (e >= -74) ? m * __uint_as_float((unsigned)(e + 75) << 23)
+                             : m * __uint_as_float((unsigned)(e + 139) << 23) *
+                                   5.421010862427522e-20f;  // 2^-64
+  return ff{h, sign ? -l : l};
+}
+
+// value m * 2^E as a double, by integer operations (selects, no branches);
+// m is an FP32 number whose magnitude stays within [2^-8, 2^8] or is zero
+// / non-finite.  Zero and underflow give +0, overflow +-inf, inf / NaN m
+// the same as a double.
 __device__ __forceinline__ double assemble(float m, int E) {
   const unsigned u = __float_as_uint(m);
   const int fe = (int)((u >> 23) & 0xffu);
-  if (fe == 0) return 0.0;
-  if (fe == 0xff) return (double)m;
+  const unsigned sign = u & 0x80000000u, mant = u & 0x7fffffu;
   const int de = fe - 127 + 1023 + E;
-  if (de <= 0) return 0.0;
-  if (de >= 2047) return (u >> 31) ? -INFINITY : INFINITY;
-  const unsigned hi = (u & 0x80000000u) | ((unsigned)de << 20) | ((u & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hi, (int)(u << 29));
+  unsigned hi = sign | ((unsigned)de << 20) | (mant >> 3), lo = u << 29;
+  const bool special = fe == 0xff;
+  const bool ovf = !special && de >= 2047;
+  const bool unf = !special && (fe == 0 || de <= 0);
+  hi = ovf ? (sign | 0x7ff00000u) : hi;
+  lo = ovf ? 0u : lo;
+  hi = special ? (sign | 0x7ff00000u | (mant >> 3)) : hi;
+  hi = unf ? 0u : hi;
+  lo = unf ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
 }
 
 // exp(x) for a float-float x, as (p, k) with exp(x) = p * 2^k,
 // p in [0.70, 1.42]
 __device__ __forceinline__ float ff_exp(ff x, int &k) {
-  if (!(fabsf(x.h) <= 3.0e3f)) {  // far outside the FP64 range, or NaN
-    if (x.h != x.h) {
-      k = 0;
-      return x.h;
-    }
-    x.h = copysignf(3.0e3f, x.h);
-    x.l = 0.0f;
-  }
-  const float t = fmaf(x.h, LOG2E_F, SHIFT_F);
+  // far outside the FP64 range: clamp (selects, no branches); NaN passes
+  const bool nan = x.h != x.h;
+  const bool big = !(fabsf(x.h) <= 3.0e3f);
+  const float xh = big ? copysignf(3.0e3f, x.h) : x.h;
+  const float xl = big ? 0.0f : x.l;
+  const float t = fmaf(xh, LOG2E_F, SHIFT_F);
   const float kf = t - SHIFT_F;
-  k = __float_as_int(t) - 0x4b400000;
-  float r = fmaf(kf, -LN2_HI_F, x.h);
+  k = nan ? 0 : __float_as_int(t) - 0x4b400000;
+  float r = fmaf(kf, -LN2_HI_F, xh);
   r = fmaf(kf, -LN2_LO_F, r);
-  r = r + x.l;
+  r = r + xl;
   float p = fmaf(r, 1.0f / 5040.0f, 1.0f / 720.0f);
   p = fmaf(p, r, 1.0f / 120.0f);
   p = fmaf(p, r, 1.0f / 24.0f);
   p = fmaf(p, r, 1.0f / 6.0f);
   p = fmaf(p, r, 0.5f);
   p = fmaf(p, r, 1.0f);
-  return fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  return nan ? x.h : p;
 }
 
 // exp of a float-float argument as a plain float (saturating)
@@ -144,12 +169,9 @@ __device__ __forceinline__ float ff_expf(ff x) {
 __device__ __forceinline__ float fsplit(float c, int &e) {
   const unsigned u = __float_as_uint(c);
   const unsigned fe = (u >> 23) & 0xffu;
-  e = (int)fe - 127;
-  if (fe == 0u) {
-    e = 0;
-    return 0.0f;
-  }
-  return __uint_as_float((u & 0x807fffffu) | 0x3f800000u);
+  const bool z = fe == 0u;  // selects, not branches: keeps callers straight-line
+  e = z ? 0 : (int)fe - 127;
+  return z ? 0.0f : __uint_as_float((u & 0x807fffffu) | 0x3f800000u);
 }
 
 struct FCol {
@@ -188,6 +210,55 @@ __device__ __forceinline__ ff rate_exponent(const Tab &t, int row,
   sign = c[6];
   return x;
 }
+
+// Exponent of the equilibrium constant of reversible reaction j (with
+// ln of its prefactor), in FP64, from the per-species Gibbs column S:
+// sum_k nu_k S_k.
+template <class DC>
+struct KcFromGibbs {
+  DC S;
+  __device__ __forceinline__ double operator()(const Tab &t, int r, int j) const {
+    double g = t.kc_lpref[j];
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) g = fma(t.nu_val[e], S[t.nu_sp[e]], g);
+    return g;
+  }
+};
+
+// The same exponent from the reaction's own polynomial in T, summed over
+// its T_common groups (rate_subs.py:592-655 forms these coefficients):
+// c0 + c1 ln T + T (c2 + T (c3 + T (c4 + c5 T))) - c6 / T, in FP64.  Needs
+// no per-state column.  KcPoly1: one group per reaction (kc_poly), the
+// prefactor folded into c0 and the T <= T_common test made on the positive
+// doubles' bit patterns as integers, so that only the polynomial's six
+// FMAs use the FP64 pipe and the code has no branch.
+struct KcPoly1 {
+  double T, logT, invT;
+  long long Tbits;
+  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
+    const double *p = t.kc_poly + 16 * j;
+    const double *c = (Tbits <= __double_as_longlong(p[0])) ? p + 2 : p + 9;
+    double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
+    h = fma(h, T, c[0]);
+    h = fma(c[1], logT, h);
+    return fma(-c[6], invT, h);
+  }
+};
+
+// Several T_common groups in a reaction: sum the groups' polynomials.
+struct KcPolyG {
+  double T, logT, invT;
+  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
+    double g = t.kc_lpref[j];
+    for (int q = t.kc_ptr[j]; q < t.kc_ptr[j + 1]; ++q) {
+      const double *c = (T <= t.kc_tmid[q]) ? t.kc_lo + 7 * q : t.kc_hi + 7 * q;
+      double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
+      h = fma(h, T, c[0]);
+      h = fma(c[1], logT, h);
+      g += fma(-c[6], invT, h);
+    }
+    return g;
+  }
+};
 
 // product of concentration factors as mantissa * 2^E
 // Product of concentration factors, times the mantissa m0 of the rate
@@ -288,12 +359,20 @@ __device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
   return low ? F * frac : F * inv1p;
 }
 
-template <int NR, int NP, int NNU, int REV, bool STAGES>
+template <int NR, int NP, int NNU, int REV, bool STAGES, class KC>
 __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
                                             int cnt, const State &s,
-                                            const FCol &C, const DCol &S,
+                                            const FCol &C, const KC &kc,
                                             const DCol &W, const Batch &b,
                                             int64_t i) {
+  // FP64 Kc exponents first: independent of the FP32 work below, so the
+  // scheduler can overlap the slow FP64 pipe with it (the block is
+  // straight-line code)
+  double g[4];
+  if (REV) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) g[u] = kc(t, rr[u], t.rev_idx[rr[u]]);
+  }
   ff x[4];
   double fwd[4], rev[4];
 #pragma unroll
@@ -319,12 +398,8 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int r = rr[u];
-      const int e0 = t.nu_ptr[r];
-      double g = t.kc_lpref[t.rev_idx[r]];  // Kc exponent in FP64
-#pragma unroll
-      for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], S[t.nu_sp[e0 + q]], g);
       int E;
-      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double(g))), E), err = 0.0f;
+      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double_int(g[u]))), E), err = 0.0f;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         int e;
@@ -355,10 +430,10 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
   }
 }
 
-template <int SH, bool STAGES>
+template <int SH, bool STAGES, class KC>
 struct Shapes {
   __device__ __forceinline__ static void run(const Tab &t, const State &s,
-                                             const FCol &C, const DCol &S,
+                                             const FCol &C, const KC &S,
                                              const DCol &W, const Batch &b,
                                              int64_t i) {
     constexpr Shape d = shape_of(SH);
@@ -370,22 +445,25 @@ struct Shapes {
       for (int u = 0; u < 4; ++u) rr[u] = t.perm[p + (u < cnt ? u : cnt - 1)];
       shape_block<d.nr, d.np, d.nnu, d.rev, STAGES>(t, rr, cnt, s, C, S, W, b, i);
     }
-    Shapes<SH + 1, STAGES>::run(t, s, C, S, W, b, i);
+    Shapes<SH + 1, STAGES, KC>::run(t, s, C, S, W, b, i);
   }
 };
-template <bool STAGES>
-struct Shapes<NSHAPE, STAGES> {
+template <bool STAGES, class KC>
+struct Shapes<NSHAPE, STAGES, KC> {
   __device__ __forceinline__ static void run(const Tab &, const State &,
-                                             const FCol &, const DCol &,
+                                             const FCol &, const KC &,
                                              const DCol &, const Batch &,
                                              int64_t) {}
 };
 
 // Net rate (fwd - rev) * pres_mod of any reaction, as FP64.
-template <class FC, class DC>
+template <class FC, class KC>
 __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
-                                          float mix, const FC &C, const DC &S,
+                                          float mix, const FC &C, const KC &kc,
                                           double &fwd, double &rev, float &pm) {
+  const int j = t.rev_idx[r];
+  // the FP64 Kc exponent first, to overlap with the FP32 forward rate
+  const double g = j >= 0 ? kc(t, r, j) : 0.0;
   float sgn;
   const ff xf = rate_exponent(t, r, s, sgn);
   int Ef;
@@ -393,15 +471,11 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   const float mf = sgn * product(pf, t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
                                  t.rx_ptr[r + 1], C, Ef);
   fwd = assemble(mf, Ef);
-  const int j = t.rev_idx[r];
   double net = fwd;
   rev = 0.0;
   if (j >= 0) {
-    double g = t.kc_lpref[j];  // Kc exponent in FP64
-    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e)
-      g = fma(t.nu_val[e], S[t.nu_sp[e]], g);
     int Er;
-    const float pr = ff_exp(ff_add(xf, ff_neg(ff_from_double(g))), Er);
+    const float pr = ff_exp(ff_add(xf, ff_neg(ff_from_double_int(g))), Er);
     const float mr = sgn * product(pr, t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r],
                                    t.px_ptr[r + 1], C, Er);
     rev = assemble(mr, Er);
@@ -416,10 +490,10 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   return net;
 }
 
-template <bool STAGES>
+template <bool STAGES, class KC>
 __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
                                         float mix, const FCol &C,
-                                        const DCol &S, const DCol &W,
+                                        const KC &S, const DCol &W,
                                         const Batch &b, int64_t i) {
   double fwd, rev;
   float pm;
@@ -436,20 +510,24 @@ __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
   }
 }
 
-template <bool STAGES>
-__global__ void __launch_bounds__(128, 1)
+// One state per thread.  Per-state shared-memory columns: C (fp32) and
+// the wdot accumulators W (FP64), 12 B per species and thread; the Kc
+// exponents come from the per-reaction polynomials (no Gibbs column, the
+// polynomials read through L1), so that 256 threads fit next to the
+// staged tables.  KC1: one T_common group per reaction (kc_poly).
+template <bool STAGES, bool KC1>
+__global__ void __launch_bounds__(256, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   Tab t;
-  int nb;
+  int nb = 0;
   if (!stage_ranges(smem, img, L, 2, &bar, b.status, t, nb)) return;
   const int N = t.N;
   const int st = blockDim.x;
   double *dbase = reinterpret_cast<double *>(smem + nb);
   const DCol W{dbase + threadIdx.x, st};
-  const DCol S{dbase + N * st + threadIdx.x, st};
-  const FCol C{reinterpret_cast<float *>(dbase + 2 * N * st) + threadIdx.x, st};
+  const FCol C{reinterpret_cast<float *>(dbase + N * st) + threadIdx.x, st};
   int bad = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -473,27 +551,27 @@ __global__ void __launch_bounds__(128, 1)
     const double yN = 1.0 - ysum;
     mwi = fma(yN, t.inv_mw[N - 1], mwi);
     const double rho = P / mwi * (s.invT * INV_RU);
-    for (int k = 0; k < N - 1; ++k)
+    for (int k = 0; k < N - 1; ++k) {
       C[k] = d2f_rn(b.Y[(int64_t)k * b.ld + i] * (rho * t.inv_mw[k]));
-    C[N - 1] = d2f_rn(yN * (rho * t.inv_mw[N - 1]));
-    // FP64 Gibbs terms
-    for (int k = 0; k < N; ++k) {
-      const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
-      const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
-      double v = fma(h, s.T, g[0]);
-      v = fma(g[1], s.logT, v);
-      S[k] = fma(g[6], s.invT, v);
       W[k] = 0.0;
     }
+    C[N - 1] = d2f_rn(yN * (rho * t.inv_mw[N - 1]));
+    W[N - 1] = 0.0;
     if (STAGES && b.conc)
       for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = (double)C[k];
     const float mix = d2f_rn(P * s.invT * INV_RU);
-    Shapes<0, STAGES>::run(t, s, C, S, W, b, i);
+    using KC = typename std::conditional<KC1, KcPoly1, KcPolyG>::type;
+    KC kc;
+    kc.T = s.T;
+    kc.logT = s.logT;
+    kc.invT = s.invT;
+    if constexpr (KC1) kc.Tbits = __double_as_longlong(s.T);
+    Shapes<0, STAGES, KC>::run(t, s, C, kc, W, b, i);
     for (int p = t.seg[NSHAPE]; p < t.R; ++p)
-      general<STAGES>(t, t.perm[p], s, mix, C, S, W, b, i);
+      general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
     for (int k = 0; k < N; ++k) {
       const double v = W[k];
-      bad += !isfinite(v);
+      bad += ((__double2hiint(v) >> 20) & 0x7ff) == 0x7ff;  // inf or NaN, integer test
       b.wdot[(int64_t)k * b.ld + i] = v;
     }
   }
@@ -593,7 +671,7 @@ __global__ void __launch_bounds__(DW * 32)
         const int r = t.dperm[p];
         double fwd, rev;
         float pm;
-        q[r] = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+        q[r] = rxn_net(t, r, s, mix, C, KcFromGibbs<DArr>{S}, fwd, rev, pm);
         if (STAGES) {
           const int jr = t.rev_idx[r], pp = t.pm_idx[r];
           if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
@@ -663,19 +741,24 @@ __global__ void __launch_bounds__(DW * 32)
 
 int grid_for(int64_t n, int block, int max_ctas);
 
-// Thread-per-state variant (kept for comparison: CRS_MODE_MIXED_TPS).
+// Thread-per-state mixed kernel (CRS_MODE_MIXED_TPS, and CRS_MODE_MIXED
+// when it fits): as many threads per CTA (multiple of 32, at most 256) as
+// the shared memory left by the tables allows.
 cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
                                   const Batch &b, int sm_count, int smem_optin,
                                   cudaStream_t s) {
-  const int block = 128;
   const size_t tab = (size_t)(L.rng[2][1] - L.rng[2][0] + L.rng[2][3] - L.rng[2][2]);
-  const size_t cols = (size_t)L.N * block * (8 + 8 + 4);
-  if (tab + cols > (size_t)smem_optin) return cudaErrorNotSupported;
+  const size_t per = (size_t)L.N * (8 + 4);
+  const long long room = (long long)smem_optin - (long long)tab;
+  int block = room > 0 ? (int)(room / (long long)per) / 32 * 32 : 0;
+  if (block > 256) block = 256;
+  if (block < 32) return cudaErrorNotSupported;
+  const size_t bytes = tab + per * block;
   const bool stages = b.conc || b.fwd || b.rev || b.pm;
-  auto k = stages ? mixed::k_wdot<true> : mixed::k_wdot<false>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(tab + cols));
-  k<<<grid_for(b.n, block, sm_count), block, tab + cols, s>>>(img, L, b);
+  auto k = L.kc_single ? (stages ? mixed::k_wdot<true, true> : mixed::k_wdot<false, true>)
+                       : (stages ? mixed::k_wdot<true, false> : mixed::k_wdot<false, false>);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
   return cudaGetLastError();
 }
 
