@@ -37,8 +37,10 @@ constexpr float LN2_HI_F = 0.693145751953125f;  // 16 significant bits
 constexpr float LN2_LO_F = 1.428606765330187e-06f;
 constexpr float SHIFT_F = 12582912.0f;          // 1.5 * 2^23
 constexpr double INV_RU = 0.0001202723625380408;
-constexpr float LN10_F = 2.302585092994046f;
-constexpr float INV_LN10_F = 0.4342944819032518f;
+constexpr float INV_LN10_F = 0.4342944920063019f;       // 1/ln 10 = INV_LN10_F + INV_LN10_LO_F
+constexpr float INV_LN10_LO_F = -1.0103049952192578e-08f;
+constexpr float LN2_H12_F = 0.693115234375f;            // ln 2, 12 significant bits
+constexpr float LN2_L12_F = 3.194618329871446e-05f;     // ln 2 - LN2_H12_F
 
 struct ff {
   float h, l;
@@ -56,6 +58,15 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
   return ff_norm(s, e);
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b);
+// a / b: one fp32 quotient, its residual a - q b in float-float, a
+// correction quotient
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float q1 = a.h / b.h;
+  const ff r = ff_add(a, ff_neg(ff_mul(b, ff{q1, 0.0f})));
+  const float q2 = r.h / b.h;
+  return ff_norm(q1, q2);
+}
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   const float p = a.h * b.h;
   float e = fmaf(a.h, b.h, -p);
@@ -331,30 +342,48 @@ __device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
     inv1p = 1.0f / (1.0f + pr);
     frac = pr * inv1p;
   }
-  // ln Pr for the broadening functions (only its log is needed there)
-  const float lnPr = (m > 0.0f) ? (float)E * 0.6931471805599453f + logf(m) : -1.0e30f;
   const int form = t.pm_form[p];
   if (form == FORM_LINDEMANN) return low ? frac : inv1p;
+  // Broadening in float-float where magnitudes demand it: log10 Pr reaches
+  // +-300, so A, B and the exponent of F are formed as float-float pairs
+  // (fp32 alone would leave F with ~1e-6 relative error).
+  // ln Pr = E ln2 + ln m (m in [1, 2)), E ln2 split as an exact 12-bit head
+  // times E plus a small tail.
+  ff lnPr = ff{-1.0e30f, 0.0f};
+  if (m > 0.0f) {
+    const float Ef = (float)E;
+    lnPr = ff_add(ff{Ef * LN2_H12_F, 0.0f}, ff{fmaf(Ef, LN2_L12_F, logf(m)), 0.0f});
+  }
   // log10(fmax(Pr, 1e-300))
-  const float lP = fmaxf(lnPr * INV_LN10_F, -300.0f);
+  ff lP = ff_mul(lnPr, ff{INV_LN10_F, INV_LN10_LO_F});
+  if (lP.h < -300.0f) lP = ff{-300.0f, 0.0f};
   float F;
   if (form == FORM_TROE) {
     const float *c = t.troe_ff + 8 * p;  // P0, -1/T3 (ff), P2, -1/T1 (ff), -T2 (ff)
     float f = c[0] * ff_expf(ff_mul(s.Tff, ff{c[1], c[2]})) +
               c[3] * ff_expf(ff_mul(s.Tff, ff{c[4], c[5]}));
     if (t.pm_troe_t2[p]) f += ff_expf(ff_mul(s.iTff, ff{c[6], c[7]}));
-    const float lF = log10f(fmaxf(f, 1.0e-37f));
-    const float A = lP - 0.67f * lF - 0.4f;
-    const float B = 0.806f - 1.1762f * lF - 0.14f * lP;
-    const float B2 = B * B;
-    F = expf(LN10_F * lF * (B2 / fmaf(A, A, B2)));
+    const float lnf = logf(fmaxf(f, 1.0e-37f));
+    const ff lF = ff_mul(ff{lnf, 0.0f}, ff{INV_LN10_F, INV_LN10_LO_F});  // log10 Fcent
+    // A = log10 Pr - 0.67 log10 Fcent - 0.4, B = 0.806 - 1.1762 log10 Fcent
+    // - 0.14 log10 Pr (rate_subs.py:993-1003)
+    const ff A = ff_add(ff_add(lP, ff_neg(ff_mul(ff{0.6700000166893005f, -1.668930060816365e-08f}, lF))),
+                        ff{-0.4000000059604645f, 5.9604645663569045e-09f});
+    const ff B = ff_add(ff_add(ff{0.8059999942779541f, 5.7220459481754915e-09f},
+                               ff_neg(ff_mul(ff{1.176200032234192f, -3.2234190427971043e-08f}, lF))),
+                        ff_neg(ff_mul(ff{0.14000000059604645f, -5.9604643443123e-10f}, lP)));
+    // F = 10^(log10 Fcent / (1 + A^2/B^2)) = exp(ln Fcent * B^2 / (A^2 + B^2))
+    const ff B2 = ff_mul(B, B);
+    const ff w = ff_div(B2, ff_add(ff_mul(A, A), B2));
+    F = ff_expf(ff_mul(ff{lnf, 0.0f}, w));
   } else {
     const float *c = t.sri_ff + 8 * p;  // a, -b (ff), -1/c (ff), d, e
-    const float X = 1.0f / (1.0f + lP * lP);
+    // X = 1 / (1 + log10^2 Pr); F = base^X
+    const ff X = ff_div(ff{1.0f, 0.0f}, ff_add(ff{1.0f, 0.0f}, ff_mul(lP, lP)));
     const float base = c[0] * ff_expf(ff_mul(s.iTff, ff{c[1], c[2]})) +
                        ff_expf(ff_mul(s.Tff, ff{c[3], c[4]}));
-    F = expf(X * logf(base));
-    if (t.pm_sri_de[p]) F *= c[5] * expf(c[6] * (s.lTff.h + s.lTff.l));
+    F = ff_expf(ff_mul(X, ff{logf(base), 0.0f}));
+    if (t.pm_sri_de[p]) F *= c[5] * ff_expf(ff_mul(ff{c[6], 0.0f}, s.lTff));
   }
   return low ? F * frac : F * inv1p;
 }
