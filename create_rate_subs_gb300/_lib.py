@@ -46,6 +46,7 @@ def _sig(lib):
         "crs_get_rxn_pres_mod_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_eval_spec_rates_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_wdot": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _i32, _vp],
+        "crs_wdot_host": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _i32],
         "crs_wdot_stages": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                             _vp, _i32, _vp],
         "crs_bind": [_vp],

@@ -66,6 +66,12 @@ struct crs_mech {
   void *d_ws = nullptr;
   int *d_escale = nullptr;
   int64_t ws_rows = 0;
+  // crs_wdot_host: two streams and two device buffers of one chunk of
+  // states each (T, P, Y, wdot), allocated on first use
+  std::mutex host_mu;
+  cudaStream_t hs[2] = {nullptr, nullptr};
+  double *d_host = nullptr;
+  int64_t host_chunk = 0;
 };
 
 namespace {
@@ -440,6 +446,57 @@ int wdot_gemm(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+// Launch the kernel of `mode` on one batch (the switch behind every
+// batched entry point).
+int launch_mode(const crs_mech *m, crs::Batch &b, int mode, cudaStream_t s) {
+  cudaError_t e;
+  switch (mode) {
+    case CRS_MODE_FP64_STRICT:
+      e = crs::launch_wdot_strict(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64:
+      // one state per thread when its columns fit on chip, else per warp
+      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      if (e == cudaErrorNotSupported)
+        e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED:
+      // one state per thread when its columns fit on chip, else per warp
+      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      if (e == cudaErrorNotSupported)
+        e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64_TPS:
+      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED_TPS:
+      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_FP64_WARP:
+      e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_MIXED_WARP:
+      e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      break;
+    case CRS_MODE_GEMM: {
+      if (b.conc || b.fwd || b.rev || b.pm)
+        return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_GEMM does not write intermediates");
+      int rc2 = wdot_gemm(const_cast<crs_mech *>(m), b, s);
+      if (rc2 != CRS_OK) return rc2;
+      e = cudaSuccess;
+      break;
+    }
+    default:
+      return fail(CRS_ERR_ARG, "unknown mode %d", mode);
+  }
+  if (e == cudaErrorNotSupported)
+    return fail(CRS_ERR_UNSUPPORTED, "mode %d is not available for this mechanism", mode);
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_wdot launch");
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *crs_last_error(void) { return g_err.c_str(); }
@@ -510,6 +567,9 @@ int crs_mech_free(crs_mech *m) {
   if (m->d_nuB) cudaFree(m->d_nuB);
   if (m->d_ws) cudaFree(m->d_ws);
   if (m->d_escale) cudaFree(m->d_escale);
+  if (m->d_host) cudaFree(m->d_host);
+  for (cudaStream_t st : m->hs)
+    if (st) cudaStreamDestroy(st);
   delete m;
   return CRS_OK;
 }
@@ -611,56 +671,73 @@ int crs_wdot_stages(const crs_mech *m, int64_t n, const double *T,
   crs::Batch b = make_batch(m, n, ld);
   b.T = T; b.P = P; b.Y = Y; b.wdot = wdot;
   b.conc = conc; b.fwd = fwd; b.rev = rev; b.pm = pres_mod;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e;
-  switch (mode) {
-    case CRS_MODE_FP64_STRICT:
-      e = crs::launch_wdot_strict(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_FP64:
-      // one state per thread when its columns fit on chip, else per warp
-      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      if (e == cudaErrorNotSupported)
-        e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_MIXED:
-      // one state per thread when its columns fit on chip, else per warp
-      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      if (e == cudaErrorNotSupported)
-        e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_FP64_TPS:
-      e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_MIXED_TPS:
-      e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_FP64_WARP:
-      e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_MIXED_WARP:
-      e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      break;
-    case CRS_MODE_GEMM: {
-      if (conc || fwd || rev || pres_mod)
-        return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_GEMM does not write intermediates");
-      int rc2 = wdot_gemm(const_cast<crs_mech *>(m), b, s);
-      if (rc2 != CRS_OK) return rc2;
-      e = cudaSuccess;
-      break;
-    }
-    default:
-      return fail(CRS_ERR_ARG, "unknown mode %d", mode);
-  }
-  if (e == cudaErrorNotSupported)
-    return fail(CRS_ERR_UNSUPPORTED, "mode %d is not available for this mechanism", mode);
-  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_wdot launch");
+  return launch_mode(m, b, mode, static_cast<cudaStream_t>(stream));
 }
 
 int crs_wdot(const crs_mech *m, int64_t n, const double *T, const double *P,
              const double *Y, int64_t ld, double *wdot, int mode, void *stream) {
   return crs_wdot_stages(m, n, T, P, Y, ld, wdot, nullptr, nullptr, nullptr,
                          nullptr, mode, stream);
+}
+
+int crs_wdot_host(const crs_mech *m, int64_t n, const double *T, const double *P,
+                  const double *Y, int64_t ld, double *wdot, int mode) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !P || !Y || !wdot) return fail(CRS_ERR_ARG, "NULL array");
+  crs_mech *mm = const_cast<crs_mech *>(m);
+  std::lock_guard<std::mutex> lock(mm->host_mu);
+  const int64_t N = m->L.N;
+  const int64_t per = 2 + (N - 1) + N;  // doubles per state: T, P, Y, wdot
+  // chunks of up to 2^17 states, at most 256 MB per buffer
+  int64_t chunk = ((int64_t)256 << 20) / (per * 8);
+  if (chunk > ((int64_t)1 << 17)) chunk = (int64_t)1 << 17;
+  if (chunk < 128) chunk = 128;
+  cudaError_t e = cudaSuccess;
+  if (mm->host_chunk < chunk) {
+    if (mm->d_host) cudaFree(mm->d_host);
+    mm->d_host = nullptr;
+    mm->host_chunk = 0;
+    e = cudaMalloc(&mm->d_host, (size_t)2 * chunk * per * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_host buffers");
+    mm->host_chunk = chunk;
+  }
+  for (int j = 0; j < 2 && e == cudaSuccess; ++j)
+    if (!mm->hs[j]) e = cudaStreamCreateWithFlags(&mm->hs[j], cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_host streams");
+  // chunk c on stream c % 2: its copies in overlap the other stream's
+  // kernel, its copies out the next kernel; a buffer is reused only after
+  // the same stream has finished with it
+  int result = CRS_OK;
+  for (int64_t c0 = 0, c = 0; c0 < n && result == CRS_OK; c0 += chunk, ++c) {
+    const int64_t cn = n - c0 < chunk ? n - c0 : chunk;
+    cudaStream_t s = mm->hs[c & 1];
+    double *dT = mm->d_host + (size_t)(c & 1) * chunk * per;
+    double *dP = dT + cn, *dY = dP + cn, *dW = dY + (N - 1) * cn;
+    const size_t row = (size_t)cn * sizeof(double);
+    e = cudaMemcpyAsync(dT, T + c0, row, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dP, P + c0, row, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && N > 1)
+      e = cudaMemcpy2DAsync(dY, row, Y + c0, (size_t)ld * sizeof(double), row, N - 1,
+                            cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      result = cuda_fail(e, "crs_wdot_host copy in");
+      break;
+    }
+    crs::Batch b = make_batch(m, cn, cn);
+    b.T = dT; b.P = dP; b.Y = dY; b.wdot = dW;
+    result = launch_mode(m, b, mode, s);
+    if (result != CRS_OK) break;
+    e = cudaMemcpy2DAsync(wdot + c0, (size_t)ld * sizeof(double), dW, row, row, N,
+                          cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) result = cuda_fail(e, "crs_wdot_host copy out");
+  }
+  for (int j = 0; j < 2; ++j) {
+    const cudaError_t es = cudaStreamSynchronize(mm->hs[j]);
+    if (es != cudaSuccess && result == CRS_OK) result = cuda_fail(es, "crs_wdot_host");
+  }
+  return result;
 }
 
 }  // extern "C"

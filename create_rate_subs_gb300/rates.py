@@ -16,8 +16,8 @@ have shape (n,), ``Y`` shape (N-1, n) or (N, n) (only the first N-1 rows
 are read), per-species / per-reaction outputs shape (rows, n).  Calls are
 ordered on torch's current CUDA stream.
 
-``wdot_host`` runs the same evaluation from host (numpy) arrays, copies
-included.
+``wdot_host`` runs the same evaluation from host arrays (numpy or CPU
+tensors) through crs_wdot_host, copies included and overlapped.
 """
 
 import ctypes
@@ -178,13 +178,42 @@ class RateSubs(object):
             _ptr(o["pm"]) if self.n_pdep else None, _lib.MODES[mode], self._stream()))
         return o
 
-    def wdot_host(self, T, P, Y, mode="fp64"):
-        """wdot from host arrays: copy in, evaluate, copy out (numpy)."""
+    def wdot_host(self, T, P, Y, mode="fp64", out=None):
+        """wdot (N, n) from host arrays, through crs_wdot_host: chunks of
+        states pass through the GPU on two streams, copies overlapping
+        kernels.  T, P: (n,), Y: (>= N-1, n) float64 numpy arrays or CPU
+        torch tensors (pinned memory lets the copies overlap); out: same
+        kinds, (N, n).  Returns out (a numpy array when allocated here)."""
         torch = _torch()
-        t = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
-             for a in (T, P, Y)]
-        w = self.wdot(t[0], t[1], t[2], mode)
-        return w.cpu().numpy()
+
+        def host(a, name, shape0=None):
+            if isinstance(a, torch.Tensor):
+                if a.is_cuda or a.dtype != torch.float64:
+                    raise ValueError("%s must be a float64 CPU tensor" % name)
+                if a.stride(-1) != 1:
+                    raise ValueError("%s must have unit state stride" % name)
+                return a, a.data_ptr(), (a.stride(0) if a.dim() == 2 else 1)
+            a = np.asarray(a)
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+            return a, a.ctypes.data, (a.shape[1] if a.ndim == 2 else 1)
+
+        T, pT, _ = host(T, "T")
+        P, pP, _ = host(P, "P")
+        Y, pY, ld = host(Y, "Y")
+        n = T.shape[0]
+        if P.shape[0] != n or Y.shape[1] != n or Y.shape[0] < self.n_species - 1:
+            raise ValueError("shapes: T (n,), P (n,), Y (>= N-1, n)")
+        if out is None:
+            out = np.empty((self.n_species, n))
+        out, pW, ldw = host(out, "out")
+        if tuple(out.shape) != (self.n_species, n) or ldw != ld:
+            raise ValueError("out must be (N, n) with the same row stride as Y")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.crs_wdot_host(self.h, n, ctypes.c_void_p(pT),
+                                              ctypes.c_void_p(pP), ctypes.c_void_p(pY), ld,
+                                              ctypes.c_void_p(pW), _lib.MODES[mode]))
+        return out
 
     def status(self):
         """(flag bits, count of non-finite wdot values) since the last reset."""

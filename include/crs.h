@@ -127,6 +127,18 @@ int crs_wdot_stages(const crs_mech *mech, int64_t n, const double *T,
                     double *wdot, double *conc, double *fwd, double *rev,
                     double *pres_mod, int mode, void *stream);
 
+/* wdot from HOST arrays (same SoA layout and ld as crs_wdot): the batched
+ * form of the reference's per-state host functions (rate_subs.py:1297-1299,
+ * 287-290, 761-763, 1124-1127 evaluated for every state).  States go
+ * through the device in chunks on two streams owned by the handle, so that
+ * the copies of one chunk overlap the kernel of the other; pinned
+ * (page-locked) host memory is needed for that overlap.  Returns when wdot
+ * is on the host.  Device buffers (<= 2 x 256 MB) are allocated on first
+ * use and kept by the handle; calls on one handle are serialised. */
+int crs_wdot_host(const crs_mech *mech, int64_t n, const double *T,
+                  const double *P, const double *Y, int64_t ld,
+                  double *wdot, int mode);
+
 /* ---- allocation-free contraction (no counterpart in the reference) ----- */
 
 /* The evaluation of crs_wdot(..., CRS_MODE_GEMM, ...) for callers that must
