@@ -56,6 +56,9 @@ def _args():
                     help="fresh states the surrogate is evaluated on")
     ap.add_argument("--sur-tol", type=float, default=0.05)
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--profile-surrogate", action="store_true",
+                    help="one surrogate network forward pass over 2^20 states "
+                         "(the case of the network-kernel ncu summary)")
     ap.add_argument("--profile", action="store_true",
                     help="one launch of each wdot kernel on 2^18 states (for ncu)")
     return ap.parse_args()
@@ -639,10 +642,30 @@ def run_profile(args):
     return 0
 
 
+def run_profile_surrogate(args):
+    """Features, the four layer GEMMs and the output kernel of the surrogate
+    network (random weights) over 2^20 states, once."""
+    import torch
+    from create_rate_subs_gb300.rates import RateSubs
+    from create_rate_subs_gb300.surrogate import Surrogate
+    torch.cuda.set_device(0)
+    rs = RateSubs(_mechanism())
+    sur = Surrogate(rs, seed=0)
+    n = 1 << 20
+    T, P, Y = sur.sample_states(n, seed=5)
+    w, nfb = sur.wdot(T, P, Y[: rs.n_species - 1].contiguous(), tol=float("inf"),
+                      with_fallback=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "surrogate network, %d states, one pass" % n}))
+    return 0
+
+
 def main():
     args = _args()
     if args.profile:
         return run_profile(args)
+    if args.profile_surrogate:
+        return run_profile_surrogate(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -100,10 +100,10 @@ constexpr size_t smem_bytes() {
 // an ST-deep ring, warp 1 lane 0 the MMAs; then all NT / 32 warps run the
 // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (the quarter its
 // rank allows) and, with NT = 256, half of the columns.  ST = 2 and NT = 256
-// let two CTAs share an SM, so one tile's epilogue overlaps the next tile's
-// loads and MMAs.
+// let two CTAs share an SM (registers capped for two), so one tile's
+// epilogue overlaps the next tile's loads and MMAs.
 template <int BN, class Epi, int ST = STAGES, int NT = 128>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, ST <= 2 ? 2 : 1)
     k_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
            int kblocks, Epi epi, int32_t *status) {
   static_assert(NT == 128 || NT == 256, "128 or 256 threads");
