@@ -47,6 +47,10 @@ def _sig(lib):
         "crs_eval_spec_rates_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_wdot": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _i32, _vp],
         "crs_wdot_host": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _i32],
+        "crs_eval_thermo_batch": [_vp, _i64, _vp, _i64, _i32, _vp, _vp],
+        "crs_eval_conc_rho_batch": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp],
+        "crs_dydt": [_vp, _i64, _vp, _vp, _i64, _vp, _i32, _i32, _vp],
+        "crs_dydt_form": [_i32],
         "crs_wdot_stages": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                             _vp, _i32, _vp],
         "crs_bind": [_vp],
@@ -74,12 +78,19 @@ def _sig(lib):
         "eval_rxn_rates": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
         "get_rxn_pres_mod": [ctypes.c_double, ctypes.c_double, _vp, _vp],
         "eval_spec_rates": [_vp, _vp, _vp, _vp, _vp],
+        "eval_h": [ctypes.c_double, _vp],
+        "eval_u": [ctypes.c_double, _vp],
+        "eval_cv": [ctypes.c_double, _vp],
+        "eval_cp": [ctypes.c_double, _vp],
+        "eval_conc_rho": [ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp],
+        "dydt": [ctypes.c_double, ctypes.c_double, _vp, _vp],
     }
     for name, args in s.items():
         f = getattr(lib, name)
         f.argtypes = args
-        f.restype = None if name in ("eval_conc", "eval_rxn_rates",
-                                     "get_rxn_pres_mod", "eval_spec_rates") else ctypes.c_int
+        f.restype = None if name in ("eval_conc", "eval_rxn_rates", "get_rxn_pres_mod",
+                                     "eval_spec_rates", "eval_h", "eval_u", "eval_cv",
+                                     "eval_cp", "eval_conc_rho", "dydt") else ctypes.c_int
     lib.crs_last_error.argtypes = []
     lib.crs_last_error.restype = ctypes.c_char_p
     return lib

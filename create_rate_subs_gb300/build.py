@@ -24,9 +24,12 @@ REPO = os.path.dirname(HERE)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
           "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include")]
-# Per-file extra flags.  The strict FP64 kernels must not contract a*b+c
-# into FMA: they reproduce the reference's operation order.
-EXTRA = {"crs_fp64_strict.cu": ["-fmad=false"]}
+# Per-file extra flags.  The strict FP64 kernels and the thermo utilities
+# must not contract a*b+c into FMA: they reproduce the reference's operation
+# order.
+EXTRA = {"crs_fp64_strict.cu": ["-fmad=false"],
+         # thermo utilities in the emitted operand order, bit for bit
+         "crs_dydt.cu": ["-fmad=false"]}
 
 
 def nvcc():

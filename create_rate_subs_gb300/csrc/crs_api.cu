@@ -175,7 +175,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       // reference-order only
       {"kc_tmid", &L.kc_tmid, 1}, {"kc_lo", &L.kc_lo, 1},
       {"kc_hi", &L.kc_hi, 1}, {"sp_lo", &L.sp_lo, 1},
-      {"sp_hi", &L.sp_hi, 1},
+      {"sp_hi", &L.sp_hi, 1}, {"sp_mw", &L.sp_mw, 1},
   };
   std::vector<unsigned char> &img = m->h_img;
   img.clear();
@@ -212,7 +212,8 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       cnt("nu_ptr") != L.R + 1 || cnt("rev_idx") != L.R ||
       cnt("pm_idx") != L.R || cnt("kc_ptr") != L.NREV + 1 ||
       cnt("pm_eff_ptr") != L.NPM + 1 || cnt("pm_kind") != L.NPM ||
-      cnt("sp_inv_mw") != L.N || cnt("sp_lo") != 7LL * L.N)
+      cnt("sp_inv_mw") != L.N || cnt("sp_lo") != 7LL * L.N ||
+      cnt("sp_hi") != 7LL * L.N || cnt("sp_mw") != L.N || cnt("sp_tmid") != L.N)
     return fail(CRS_ERR_BLOB, "table sizes disagree with dims");
   if (!ptr_ok(t.rx_ptr, L.R, cnt("rx_sp")) || !ptr_ok(t.px_ptr, L.R, cnt("px_sp")) ||
       !ptr_ok(t.nu_ptr, L.R, cnt("nu_sp")) ||
@@ -310,6 +311,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   raw(&IL::rate_par, "rate_par"); raw(&IL::kc_pref, "kc_pref");
   raw(&IL::pm_troe, "pm_troe"); raw(&IL::pm_sri, "pm_sri");
   raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
+  raw(&IL::sp_mw, "sp_mw"); der(&IL::sp_thermo);
   // every blob section and every derived table must have been placed
   for (auto &w : want) {
     bool found = false;
@@ -680,6 +682,64 @@ int crs_wdot(const crs_mech *m, int64_t n, const double *T, const double *P,
                          nullptr, mode, stream);
 }
 
+int crs_eval_thermo_batch(const crs_mech *m, int64_t n, const double *T, int64_t ld,
+                          int which, double *out, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (which < 0 || which > 3) return fail(CRS_ERR_ARG, "which must be 0..3 (h, u, cv, cp)");
+  if (n == 0) return CRS_OK;
+  if (!T || !out) return fail(CRS_ERR_ARG, "NULL array");
+  cudaError_t e = crs::launch_thermo(m->d_img, m->L, which, n, T, ld, out, m->sm_count,
+                                     static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_eval_thermo_batch");
+}
+
+int crs_eval_conc_rho_batch(const crs_mech *m, int64_t n, const double *T, const double *rho,
+                            const double *Y, int64_t ld, double *y_N, double *mw_avg,
+                            double *pres, double *conc, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (n == 0) return CRS_OK;
+  if (!T || !rho || !Y) return fail(CRS_ERR_ARG, "NULL array");
+  cudaError_t e = crs::launch_conc_rho(m->d_img, m->L, n, T, rho, Y, ld, y_N, mw_avg, pres,
+                                       conc, m->sm_count, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_eval_conc_rho_batch");
+}
+
+int crs_dydt(const crs_mech *m, int64_t n, const double *p_or_rho, const double *y,
+             int64_t ld, double *dy, int conv, int mode, void *stream) {
+  int rc = check_batch(m, n, ld);
+  if (rc) return rc;
+  if (conv != 0 && conv != 1) return fail(CRS_ERR_ARG, "conv must be 0 or 1");
+  if (n == 0) return CRS_OK;
+  if (!p_or_rho || !y || !dy) return fail(CRS_ERR_ARG, "NULL array");
+  const int64_t N = m->L.N;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // stream-ordered scratch: wdot [N][ld] and, for constant volume, the
+  // pressure row
+  double *ws = nullptr;
+  const size_t bytes = ((size_t)N * ld + (conv ? (size_t)ld : 0)) * sizeof(double);
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&ws), bytes, s);
+  if (e != cudaSuccess) return cuda_fail(e, "crs_dydt scratch");
+  double *W = ws, *Pw = ws + (size_t)N * ld;
+  if (conv)
+    e = crs::launch_conc_rho(m->d_img, m->L, n, y, p_or_rho, y + ld, ld, nullptr, nullptr, Pw,
+                             nullptr, m->sm_count, s);
+  int result = e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_dydt pressure");
+  if (result == CRS_OK) {
+    crs::Batch b = make_batch(m, n, ld);
+    b.T = y; b.P = conv ? Pw : p_or_rho; b.Y = y + ld; b.wdot = W;
+    result = launch_mode(m, b, mode, s);
+  }
+  if (result == CRS_OK) {
+    e = crs::launch_dydt_finish(m->d_img, m->L, conv, n, y, ld, p_or_rho, W, dy, m->sm_count, s);
+    if (e != cudaSuccess) result = cuda_fail(e, "crs_dydt");
+  }
+  e = cudaFreeAsync(ws, s);
+  if (e != cudaSuccess && result == CRS_OK) result = cuda_fail(e, "crs_dydt scratch");
+  return result;
+}
+
 int crs_wdot_host(const crs_mech *m, int64_t n, const double *T, const double *P,
                   const double *Y, int64_t ld, double *wdot, int mode) {
   int rc = check_batch(m, n, ld);
@@ -912,6 +972,97 @@ void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
   }
   for (int k = 0; k < L.N - 1; ++k) sp_rates[k] = w[k];
   *dy_N = w[L.N - 1];
+}
+
+namespace {
+int g_dydt_conv = 0;  // form of the per-state dydt (crs_dydt_form)
+
+void thermo_one(int which, const char *name, double T, double *out) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "%s: no mechanism bound (crs_bind)", name);
+    return;
+  }
+  One o = layout(m, g_bound.d);
+  const int N = m->L.N;
+  cudaError_t e = cudaMemcpy(o.T, &T, sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = crs::launch_thermo(m->d_img, m->L, which, 1, o.T, 1, o.w, m->sm_count, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, name);
+    fill_nan(out, N);
+  }
+}
+}  // namespace
+
+// rate_subs.py:1497-1776 (chem_utils.h :1276-1279)
+void eval_h(const double T, double *h) { thermo_one(0, "eval_h", T, h); }
+void eval_u(const double T, double *u) { thermo_one(1, "eval_u", T, u); }
+void eval_cv(const double T, double *cv) { thermo_one(2, "eval_cv", T, cv); }
+void eval_cp(const double T, double *cp) { thermo_one(3, "eval_cp", T, cp); }
+
+// rate_subs.py:1396-1490 (chem_utils.h :1274-1275)
+void eval_conc_rho(const double T, const double rho, const double *y, double *y_N,
+                   double *mw_avg, double *pres, double *conc) {
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "eval_conc_rho: no mechanism bound (crs_bind)");
+    return;
+  }
+  One o = layout(m, g_bound.d);
+  const int N = m->L.N;
+  double tr[2] = {T, rho};
+  cudaError_t e = cudaMemcpy(o.T, tr, sizeof tr, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && N > 1)
+    e = cudaMemcpy(o.C, y, (N - 1) * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = crs::launch_conc_rho(m->d_img, m->L, 1, o.T, o.P, o.C, 1, o.misc, o.misc + 1,
+                             o.misc + 2, o.w, m->sm_count, 0);
+  double misc[3];
+  if (e == cudaSuccess) e = cudaMemcpy(conc, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(misc, o.misc, sizeof misc, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "eval_conc_rho");
+    fill_nan(conc, N);
+    misc[0] = misc[1] = misc[2] = __builtin_nan("");
+  }
+  *y_N = misc[0];
+  *mw_avg = misc[1];
+  *pres = misc[2];
+}
+
+int crs_dydt_form(int conv) {
+  if (conv != 0 && conv != 1) return fail(CRS_ERR_ARG, "conv must be 0 or 1");
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  g_dydt_conv = conv;
+  return CRS_OK;
+}
+
+// rate_subs.py:1829-2067 (dydt.h): y = [T, Y_0 .. Y_{N-2}]; `pres` is the
+// pressure (constant pressure, the default) or the density (constant
+// volume, after crs_dydt_form(1)), as the emitted CONP / CONV builds read it.
+void dydt(const double t, const double pres, const double *y, double *dy) {
+  (void)t;
+  std::lock_guard<std::mutex> lk(g_bound.mu);
+  const crs_mech *m = g_bound.m;
+  if (!m) {
+    fail(CRS_ERR_NOMECH, "dydt: no mechanism bound (crs_bind)");
+    return;
+  }
+  One o = layout(m, g_bound.d);
+  const int N = m->L.N;
+  cudaError_t e = cudaMemcpy(o.P, &pres, sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(o.C, y, N * sizeof(double), cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? CRS_OK : cuda_fail(e, "dydt");
+  if (rc == CRS_OK)
+    rc = crs_dydt(m, 1, o.P, o.C, 1, o.w, g_dydt_conv, CRS_MODE_FP64_STRICT, nullptr);
+  if (rc == CRS_OK) {
+    e = cudaMemcpy(dy, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "dydt");
+  }
+  if (rc != CRS_OK) fill_nan(dy, N);
 }
 
 }  // extern "C"

@@ -110,6 +110,25 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
     }
   }
   put(extra, &ImgLayout::kc_poly, kp);
+  // thermo utilities: RU/mw, mw, T_common and the NASA-7 coefficients in the
+  // forms the emitted eval_h/u/cv/cp print (rate_subs.py:1513-1776)
+  std::vector<double> th(24 * (size_t)L.N, 0.0);
+  for (int k = 0; k < L.N; ++k) {
+    double *o = th.data() + 24 * k;
+    o[0] = 8314.4621 / t.sp_mw[k];  // chem.RU / mw, as the emitter prints it
+    o[1] = t.sp_mw[k];
+    o[2] = t.sp_tmid[k];
+    for (int h = 0; h < 2; ++h) {
+      const double *a = (h ? t.sp_hi : t.sp_lo) + 7 * k;
+      double *c = o + 4 + 10 * h;
+      for (int j = 0; j < 6; ++j) c[j] = a[j];
+      c[6] = a[1] / 2.0;
+      c[7] = a[2] / 3.0;
+      c[8] = a[3] / 4.0;
+      c[9] = a[4] / 5.0;
+    }
+  }
+  put(extra, &ImgLayout::sp_thermo, th);
   put(extra, &ImgLayout::troe_x, tx);
   put(extra, &ImgLayout::sri_x, sx);
   put(extra, &ImgLayout::sp_gibbs, g);

@@ -45,6 +45,9 @@ struct ImgLayout {
   // exponent polynomial with ln(prefactor) folded into c0; built when every
   // reaction has a single T_common group (kc_single = 1)
   int kc_poly, kc_single;
+  // derived f64 section (thermo utilities): per species 24 doubles
+  // [RU/mw, mw, T_common, 0, lo: a0..a5, a1/2, a2/3, a3/4, a4/5, hi: same]
+  int sp_thermo;
   // derived i32 sections: reaction processing order, start of each shape
   // group in it (crs_shapes.cuh), expanded reactant / product factors
   int perm, seg, rfac, pfac;
@@ -54,7 +57,7 @@ struct ImgLayout {
   int dperm, spc_ptr, spc_r, spc_nu, lane_ptr, lane_sp;
   // f64 sections
   int inv_mw, rate_par, rx_nu, px_nu, kc_tmid, kc_lo, kc_hi, kc_pref,
-      pm_eff_val, pm_troe, pm_sri, nu_val, sp_tmid, sp_lo, sp_hi, kc_dnu;
+      pm_eff_val, pm_troe, pm_sri, nu_val, sp_tmid, sp_lo, sp_hi, kc_dnu, sp_mw;
   // i32 sections
   int rate_kind, rate_npow, rx_ptr, rx_sp, rx_nint, px_ptr, px_sp, px_nint,
       rev_idx, kc_ptr, pm_idx, pm_kind, pm_form, pm_sp, pm_eff_ptr,
@@ -67,11 +70,11 @@ struct Tab {
   const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
   const double *spc_nu;
   const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
-  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly;
+  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly, *sp_thermo;
   int kc_single;
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
-      *sp_hi, *kc_dnu;
+      *sp_hi, *kc_dnu, *sp_mw;
   const int32_t *rate_kind, *rate_npow, *rx_ptr, *rx_sp, *rx_nint, *px_ptr,
       *px_sp, *px_nint, *rev_idx, *kc_ptr, *pm_idx, *pm_kind, *pm_form,
       *pm_sp, *pm_eff_ptr, *pm_eff_sp, *pm_k0, *pm_kinf, *pm_troe_t2,
@@ -95,7 +98,7 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
 #define CRS_S(x) t.x = reinterpret_cast<const float *>(CRS_P(x))
 #define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
   CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
-  CRS_F(exptab); CRS_F(kc_poly);
+  CRS_F(exptab); CRS_F(kc_poly); CRS_F(sp_thermo);
   CRS_I(perm); CRS_I(seg); CRS_I(rfac); CRS_I(pfac);
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
@@ -103,7 +106,7 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
   CRS_F(inv_mw); CRS_F(rate_par); CRS_F(rx_nu); CRS_F(px_nu); CRS_F(kc_tmid);
   CRS_F(kc_lo); CRS_F(kc_hi); CRS_F(kc_pref); CRS_F(pm_eff_val);
   CRS_F(pm_troe); CRS_F(pm_sri); CRS_F(nu_val); CRS_F(sp_tmid); CRS_F(sp_lo);
-  CRS_F(sp_hi); CRS_F(kc_dnu);
+  CRS_F(sp_hi); CRS_F(kc_dnu); CRS_F(sp_mw);
   CRS_I(rate_kind); CRS_I(rate_npow); CRS_I(rx_ptr); CRS_I(rx_sp);
   CRS_I(rx_nint); CRS_I(px_ptr); CRS_I(px_sp); CRS_I(px_nint); CRS_I(rev_idx);
   CRS_I(kc_ptr); CRS_I(pm_idx); CRS_I(pm_kind); CRS_I(pm_form); CRS_I(pm_sp);
@@ -239,6 +242,22 @@ __device__ inline bool stage_ranges(unsigned char *smem,
 }
 
 #endif
+
+// Thermo utilities and the ODE right-hand side (crs_dydt.cu).
+// which: 0 h, 1 u, 2 cv, 3 cp (per species, [N][ld]).
+cudaError_t launch_thermo(const unsigned char *img, const ImgLayout &L, int which, int64_t n,
+                          const double *T, int64_t ld, double *out, int sm_count,
+                          cudaStream_t s);
+// eval_conc_rho over n states; any output may be NULL.
+cudaError_t launch_conc_rho(const unsigned char *img, const ImgLayout &L, int64_t n,
+                            const double *T, const double *rho, const double *Y, int64_t ld,
+                            double *y_N, double *mw_avg, double *pres, double *conc,
+                            int sm_count, cudaStream_t s);
+// dy from y = [T; Y_0..Y_{N-2}] ([N][ld]) and wdot W ([N][ld]): the energy
+// equation and dY/dt; conv = 1: p_or_rho is the density, else the pressure.
+cudaError_t launch_dydt_finish(const unsigned char *img, const ImgLayout &L, int conv,
+                               int64_t n, const double *y, int64_t ld, const double *p_or_rho,
+                               const double *W, double *dy, int sm_count, cudaStream_t s);
 
 // Sets the text returned by crs_last_error() and returns code.
 int report(int code, const char *msg);

@@ -10,6 +10,9 @@ evaluates a whole batch of states held on the GPU:
 * ``get_rxn_pres_mod(T, P, C)``   -> pres_mod
 * ``eval_spec_rates(fwd, rev, pres_mod)`` -> wdot (row N-1 = dy_N)
 * ``wdot(T, P, Y, mode)``         -> the fused hot path
+* ``eval_h/u/cv/cp(T)``, ``eval_conc_rho(T, rho, Y)``, ``dydt(P or rho,
+  y, conv)`` -> the thermo utilities and ODE right-hand side
+  (rate_subs.py:1396-2067)
 
 Arrays are torch CUDA tensors in structure-of-arrays layout: ``T`` and ``P``
 have shape (n,), ``Y`` shape (N-1, n) or (N, n) (only the first N-1 rows
@@ -145,6 +148,65 @@ class RateSubs(object):
             self.h, n, _ptr(fwd), _ptr(rev) if self.n_rev else None,
             _ptr(pres_mod) if self.n_pdep else None, n, _ptr(w), self._stream()))
         return w
+
+    # -- thermo utilities and the ODE right-hand side (rate_subs.py:1396-2067)
+    def _thermo(self, which, T):
+        torch = _torch()
+        if T.dtype != torch.float64 or T.dim() != 1 or not T.is_cuda or T.stride(0) != 1:
+            raise ValueError("T must be a contiguous 1-D float64 CUDA tensor")
+        n = T.shape[0]
+        out = self._out(self.n_species, n)
+        _lib.check(self.lib.crs_eval_thermo_batch(self.h, n, _ptr(T), n, which, _ptr(out),
+                                                  self._stream()))
+        return out
+
+    def eval_h(self, T):
+        """Species enthalpies h (N, n) [J/kg]."""
+        return self._thermo(0, T)
+
+    def eval_u(self, T):
+        """Species internal energies u (N, n) [J/kg]."""
+        return self._thermo(1, T)
+
+    def eval_cv(self, T):
+        """Species cv (N, n) [J/(kg K)]."""
+        return self._thermo(2, T)
+
+    def eval_cp(self, T):
+        """Species cp (N, n) [J/(kg K)]."""
+        return self._thermo(3, T)
+
+    def eval_conc_rho(self, T, rho, Y):
+        """(y_N, mw_avg, pres, conc) from density, as eval_conc_rho."""
+        n, ld = self._check_states(T, rho, Y)
+        torch = _torch()
+        misc = torch.empty((3, n), dtype=torch.float64, device=self.device)
+        conc = self._out(self.n_species, n)
+        _lib.check(self.lib.crs_eval_conc_rho_batch(
+            self.h, n, _ptr(T), _ptr(rho), _ptr(Y), ld, _ptr(misc[0]), _ptr(misc[1]),
+            _ptr(misc[2]), _ptr(conc), self._stream()))
+        return misc[0], misc[1], misc[2], conc
+
+    def dydt(self, p_or_rho, y, conv=False, mode="fp64", out=None):
+        """dy (N, n) for the emitted state vector y (N, n) = [T; Y_0..Y_{N-2}]:
+        constant pressure (p_or_rho = P) or constant volume (conv=True,
+        p_or_rho = rho); wdot from `mode`."""
+        torch = _torch()
+        if y.dtype != torch.float64 or y.dim() != 2 or not y.is_cuda or y.stride(1) != 1:
+            raise ValueError("y must be a (species, n) float64 CUDA tensor")
+        n = y.shape[1]
+        if y.shape[0] != self.n_species or p_or_rho.shape != (n,):
+            raise ValueError("y must be (N, n) and p_or_rho (n,)")
+        p = p_or_rho.contiguous()
+        ld = y.stride(0)
+        if out is None:
+            out = torch.empty((self.n_species, ld), dtype=torch.float64,
+                              device=self.device)[:, :n]
+        elif out.stride(0) != ld or out.stride(1) != 1:
+            raise ValueError("out must have the row stride of y")
+        _lib.check(self.lib.crs_dydt(self.h, n, _ptr(p), _ptr(y), ld, _ptr(out),
+                                     int(bool(conv)), _lib.MODES[mode], self._stream()))
+        return out
 
     # -- fused hot path ----------------------------------------------------
     def wdot(self, T, P, Y, mode="fp64", out=None):

@@ -127,6 +127,29 @@ int crs_wdot_stages(const crs_mech *mech, int64_t n, const double *T,
                     double *wdot, double *conc, double *fwd, double *rev,
                     double *pres_mod, int mode, void *stream);
 
+/* ---- thermo utilities and the ODE right-hand side ------------------------ */
+
+/* eval_h / eval_u / eval_cv / eval_cp over n states (rate_subs.py:1497-1776):
+ * which 0 h [J/kg], 1 u [J/kg], 2 cv [J/(kg K)], 3 cp; out [N][ld]. */
+int crs_eval_thermo_batch(const crs_mech *mech, int64_t n, const double *T,
+                          int64_t ld, int which, double *out, void *stream);
+/* eval_conc_rho over n states (rate_subs.py:1396-1490): concentrations and
+ * pressure from density; y_N, mw_avg, pres, conc may be NULL. */
+int crs_eval_conc_rho_batch(const crs_mech *mech, int64_t n, const double *T,
+                            const double *rho, const double *Y, int64_t ld,
+                            double *y_N, double *mw_avg, double *pres,
+                            double *conc, void *stream);
+/* dydt over n states (rate_subs.py:1829-2067): y [N][ld] holds T in row 0
+ * and Y_0..Y_{N-2} in rows 1..N-1 (the emitted state vector), dy the same
+ * (dT/dt, dY_k/dt).  conv = 0: constant pressure, p_or_rho[n] = P [Pa];
+ * conv = 1: constant volume, p_or_rho = rho [kg/m^3] (the form the
+ * reference means; its emitted constant-volume text does not compile).
+ * wdot comes from `mode` (CRS_MODE_*); the energy equation is FP64.  Uses
+ * N*ld (+ ld) doubles of stream-ordered scratch (cudaMallocAsync). */
+int crs_dydt(const crs_mech *mech, int64_t n, const double *p_or_rho,
+             const double *y, int64_t ld, double *dy, int conv, int mode,
+             void *stream);
+
 /* wdot from HOST arrays (same SoA layout and ld as crs_wdot): the batched
  * form of the reference's per-state host functions (rate_subs.py:1297-1299,
  * 287-290, 761-763, 1124-1127 evaluated for every state).  States go
@@ -290,6 +313,22 @@ void get_rxn_pres_mod(const double T, const double pres, const double *C,
 /* rate_subs.py:1124-1127 (rates.h) */
 void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
                      const double *pres_mod, double *sp_rates, double *dy_N);
+
+/* rate_subs.py:1497-1776 (chem_utils.h): per-species h, u, cv, cp at T */
+void eval_h(const double T, double *h);
+void eval_u(const double T, double *u);
+void eval_cv(const double T, double *cv);
+void eval_cp(const double T, double *cp);
+/* rate_subs.py:1396-1490 (chem_utils.h) */
+void eval_conc_rho(const double T, const double rho, const double *y,
+                   double *y_N, double *mw_avg, double *pres, double *conc);
+/* rate_subs.py:1829-2067 (dydt.h): y = [T, Y_0 .. Y_{N-2}], dy the same;
+ * `pres` is the pressure (constant pressure, the default) or the density
+ * after crs_dydt_form(1) (constant volume), as the emitted -DCONP / -DCONV
+ * builds read it.  Uses CRS_MODE_FP64_STRICT for wdot. */
+void dydt(const double t, const double pres, const double *y, double *dy);
+/* Form of the per-state dydt: 0 constant pressure, 1 constant volume. */
+int crs_dydt_form(int conv);
 
 #ifdef __cplusplus
 }

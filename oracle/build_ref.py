@@ -10,13 +10,15 @@ Recipe, two steps:
     ``range`` in create_rate_subs.py), runs the reference's
     ``create_rate_subs('c', mech, therm)`` in a scratch working directory
     and copies the emitted ``chem_utils.c``, ``rxn_rates.c``,
-    ``rxn_rates_pres_mod.c``, ``spec_rates.c`` and their headers into
+    ``rxn_rates_pres_mod.c``, ``spec_rates.c``, ``dydt.c`` and their headers into
     ``oracle/_ref/<name>/``.  Nothing is written to the reference checkout.
 
 ``compile``  (needs only ``oracle/_ref/<name>/`` and ``oracle/ref_harness.c``)
     Compiles the emitted files with the batch driver into
     ``oracle/_ref/<name>/libref.so`` (``-O2 -ffp-contract=off``: the parity
-    build) and ``libref_omp.so`` (``-O3 -fopenmp``: the timed CPU baseline).
+    build) and ``libref_omp.so`` (``-O3 -fopenmp``: the timed CPU baseline),
+    and the emitted ``dydt.c`` (constant pressure, ``-DCONP``) with
+    ``ref_dydt_harness.c`` into ``libref_dydt.so``.
 
 ``oracle/_ref/`` is git-ignored; the emitted sources travel with the
 working tree so that ``compile`` can run on another host.
@@ -36,7 +38,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REF_OUT = os.path.join(HERE, "_ref")
 EMITTED = ("chem_utils.c", "rxn_rates.c", "rxn_rates_pres_mod.c",
-           "spec_rates.c", "header.h", "rates.h", "chem_utils.h")
+           "spec_rates.c", "header.h", "rates.h", "chem_utils.h", "dydt.c",
+           "dydt.h")
 
 _PATCHES = {
     "chem_utilities.py": [("except Exception, e:", "except Exception as e:"),
@@ -148,6 +151,11 @@ def compile_ref(name, opt_parity=None, opt_fast=None):
              + srcs + [harness, "-lm"]),
             (base + [opt_fast, "-fopenmp", "-o", "libref_omp.so"]
              + srcs + [harness, "-lm"])]
+    if os.path.exists(os.path.join(d, "dydt.c")):
+        # the emitted constant-pressure dydt (its CONV branch does not compile)
+        jobs.append(base + ["-DCONP", opt_parity, "-ffp-contract=off", "-o",
+                            "libref_dydt.so"] + srcs
+                    + ["dydt.c", os.path.join(HERE, "ref_dydt_harness.c"), "-lm"])
     procs = [subprocess.Popen(j, cwd=d, stdout=subprocess.PIPE,
                               stderr=subprocess.STDOUT, text=True)
              for j in jobs]

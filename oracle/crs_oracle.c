@@ -14,6 +14,14 @@
  *   oracle_eval_rxn_rates    rate_subs.py:283-704 (rate constants :20-135)
  *   oracle_get_rxn_pres_mod  rate_subs.py:757-1073
  *   oracle_eval_spec_rates   rate_subs.py:1121-1235
+ *   oracle_thermo            eval_h / eval_u / eval_cv / eval_cp,
+ *                            rate_subs.py:1497-1776
+ *   oracle_eval_conc_rho     rate_subs.py:1396-1490
+ *   oracle_dydt              dydt, constant pressure rate_subs.py:1829-1946
+ *                            and constant volume :1951-2067 (the constant
+ *                            volume branch as its emitter means it: the
+ *                            emitted text misses a comma at :1967-1969 and a
+ *                            '+' at :2024-2025 and does not compile)
  */
 #include <math.h>
 #include <stdint.h>
@@ -43,6 +51,7 @@ typedef struct {
   const double *pm_eff_val, *pm_troe, *pm_sri;
   const int32_t *nu_ptr, *nu_sp;
   const double *nu_val;
+  const double *sp_mw, *sp_tmid, *sp_lo, *sp_hi;
   unsigned char *blob; /* owned copy */
 } omech;
 
@@ -101,10 +110,12 @@ int oracle_load(const void *blob, size_t n, omech **out) {
   I32(pm_troe_t2, "pm_troe_t2"); I32(pm_sri_de, "pm_sri_de");
   F64(pm_eff_val, "pm_eff_val"); F64(pm_troe, "pm_troe"); F64(pm_sri, "pm_sri");
   I32(nu_ptr, "nu_ptr"); I32(nu_sp, "nu_sp"); F64(nu_val, "nu_val");
+  F64(sp_mw, "sp_mw"); F64(sp_tmid, "sp_tmid"); F64(sp_lo, "sp_lo"); F64(sp_hi, "sp_hi");
 #undef F64
 #undef I32
   if (!m->inv_mw || !m->rate_kind || !m->rx_ptr || !m->px_ptr || !m->rev_idx ||
-      !m->pm_idx || !m->nu_ptr || !m->kc_ptr || !m->pm_eff_ptr) {
+      !m->pm_idx || !m->nu_ptr || !m->kc_ptr || !m->pm_eff_ptr || !m->sp_mw ||
+      !m->sp_tmid || !m->sp_lo || !m->sp_hi) {
     oracle_free(m);
     return 3;
   }
@@ -357,4 +368,147 @@ int oracle_wdot_omp(const omech *m, int64_t n, const double *T,
     one_state(m, i, T, P, Y, ld, NULL, NULL, NULL, NULL, wdot, NULL);
 #endif
   return used;
+}
+
+
+/* ---- thermodynamic utilities and the ODE right-hand side ---------------- */
+
+#define RU_J 8314.4621 /* chem.RU, J/(kmol K) */
+
+/* Per-species h [J/kg] (which 0), u (1), cv [J/(kg K)] (2), cp (3) at T, in
+ * the emitted form: RU/mw times a Horner polynomial whose coefficients are
+ * the NASA-7 a_j, divided by 2..5 for h and u (rate_subs.py:1513-1776). */
+void oracle_thermo(const omech *m, int which, double T, double *out) {
+  for (int k = 0; k < m->N; ++k) {
+    const double *a = (T <= m->sp_tmid[k]) ? m->sp_lo + 7 * k : m->sp_hi + 7 * k;
+    const double rm = RU_J / m->sp_mw[k];
+    double v;
+    switch (which) {
+      case 0:
+        v = rm * (a[5] + T * (a[0] + T * (a[1] / 2.0 + T * (a[2] / 3.0 +
+                  T * (a[3] / 4.0 + a[4] / 5.0 * T)))));
+        break;
+      case 1:
+        v = rm * (a[5] + T * (a[0] - 1.0 + T * (a[1] / 2.0 + T * (a[2] / 3.0 +
+                  T * (a[3] / 4.0 + a[4] / 5.0 * T)))));
+        break;
+      case 2:
+        v = rm * (a[0] - 1.0 + T * (a[1] + T * (a[2] + T * (a[3] + a[4] * T))));
+        break;
+      default:
+        v = rm * (a[0] + T * (a[1] + T * (a[2] + T * (a[3] + a[4] * T))));
+        break;
+    }
+    out[k] = v;
+  }
+}
+
+/* eval_conc_rho: concentrations and pressure from density (:1396-1490). */
+void oracle_eval_conc_rho(const omech *m, double T, double rho, const double *y,
+                          double *y_N, double *mw_avg, double *pres,
+                          double *conc) {
+  int N = m->N;
+  double s = y[0];
+  for (int k = 1; k < N - 1; ++k) s = s + y[k];
+  *y_N = (N > 1) ? 1.0 - s : 1.0;
+  double mw = 0.0;
+  for (int k = 0; k < N - 1; ++k) {
+    double t = y[k] * m->inv_mw[k];
+    mw = (k == 0) ? t : mw + t;
+  }
+  mw = (N > 1) ? mw + (*y_N) * m->inv_mw[N - 1] : (*y_N) * m->inv_mw[N - 1];
+  *mw_avg = 1.0 / mw;
+  *pres = rho * 8.31446210e+03 * T / (*mw_avg);
+  for (int k = 0; k < N - 1; ++k) conc[k] = rho * y[k] * m->inv_mw[k];
+  conc[N - 1] = rho * (*y_N) * m->inv_mw[N - 1];
+}
+
+/* dydt for y = [T, Y_0 .. Y_{N-2}] and dy the same; conv = 0: p_or_rho is
+ * the pressure (constant pressure, cp and h), conv = 1: the density
+ * (constant volume, cv and u). */
+void oracle_dydt(const omech *m, int conv, double p_or_rho, const double *y,
+                 double *dy) {
+  const int N = m->N;
+  double *C = (double *)alloca(sizeof(double) * N);
+  double *fwd = (double *)alloca(sizeof(double) * (m->R + 1));
+  double *rev = (double *)alloca(sizeof(double) * (m->NREV + 1));
+  double *pm = (double *)alloca(sizeof(double) * (m->NPM + 1));
+  double *c = (double *)alloca(sizeof(double) * N);
+  double *e = (double *)alloca(sizeof(double) * N);
+  const double T = y[0];
+  double y_N, mw_avg, rho, pres;
+  if (conv) {
+    rho = p_or_rho;
+    oracle_eval_conc_rho(m, T, rho, y + 1, &y_N, &mw_avg, &pres, C);
+  } else {
+    pres = p_or_rho;
+    oracle_eval_conc(m, T, pres, y + 1, &y_N, &mw_avg, &rho, C);
+  }
+  oracle_eval_rxn_rates(m, T, pres, C, fwd, rev);
+  oracle_get_rxn_pres_mod(m, T, pres, C, pm);
+  double dy_N;
+  oracle_eval_spec_rates(m, fwd, rev, pm, dy + 1, &dy_N);
+  oracle_thermo(m, conv ? 2 : 3, T, c);
+  double avg = 0.0;
+  for (int k = 0; k < N - 1; ++k) {
+    double t = c[k] * y[k + 1];
+    avg = (k == 0) ? t : avg + t;
+  }
+  avg = (N > 1) ? avg + c[N - 1] * y_N : c[N - 1] * y_N;
+  oracle_thermo(m, conv ? 1 : 0, T, e);
+  double sum = 0.0;
+  for (int k = 0; k < N - 1; ++k) {
+    double t = dy[k + 1] * e[k] * m->sp_mw[k];
+    sum = (k == 0) ? t : sum + t;
+  }
+  sum = (N > 1) ? sum + dy_N * e[N - 1] * m->sp_mw[N - 1] : dy_N * e[N - 1] * m->sp_mw[N - 1];
+  dy[0] = (-1.0 / (rho * avg)) * sum;
+  for (int k = 0; k < N - 1; ++k) dy[k + 1] *= (m->sp_mw[k] / rho);
+}
+
+/* SoA batches: y and dy [N][ld], thermo out [N][ld], misc (y_N, mw_avg,
+ * pres) [3][ld]. */
+int oracle_dydt_batch(const omech *m, int conv, int64_t n, const double *p_or_rho,
+                      const double *y, int64_t ld, double *dy) {
+  if (!m || n < 0 || ld < n) return 1;
+  const int N = m->N;
+  double *ys = (double *)malloc(sizeof(double) * 2 * N);
+  double *ds = ys + N;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int k = 0; k < N; ++k) ys[k] = y[(int64_t)k * ld + i];
+    oracle_dydt(m, conv, p_or_rho[i], ys, ds);
+    for (int k = 0; k < N; ++k) dy[(int64_t)k * ld + i] = ds[k];
+  }
+  free(ys);
+  return 0;
+}
+
+int oracle_thermo_batch(const omech *m, int which, int64_t n, const double *T,
+                        int64_t ld, double *out) {
+  if (!m || n < 0 || ld < n || which < 0 || which > 3) return 1;
+  double *v = (double *)malloc(sizeof(double) * m->N);
+  for (int64_t i = 0; i < n; ++i) {
+    oracle_thermo(m, which, T[i], v);
+    for (int k = 0; k < m->N; ++k) out[(int64_t)k * ld + i] = v[k];
+  }
+  free(v);
+  return 0;
+}
+
+int oracle_conc_rho_batch(const omech *m, int64_t n, const double *T,
+                          const double *rho, const double *Y, int64_t ld,
+                          double *misc, double *conc) {
+  if (!m || n < 0 || ld < n) return 1;
+  const int N = m->N;
+  double *y = (double *)malloc(sizeof(double) * 2 * N);
+  double *c = y + N;
+  for (int64_t i = 0; i < n; ++i) {
+    double y_N, mw, p;
+    for (int k = 0; k < N - 1; ++k) y[k] = Y[(int64_t)k * ld + i];
+    oracle_eval_conc_rho(m, T[i], rho[i], y, &y_N, &mw, &p, c);
+    if (conc) for (int k = 0; k < N; ++k) conc[(int64_t)k * ld + i] = c[k];
+    if (misc) { misc[i] = y_N; misc[ld + i] = mw; misc[2 * ld + i] = p; }
+  }
+  free(y);
+  return 0;
 }

@@ -22,6 +22,7 @@ SRC = os.path.join(HERE, "crs_oracle.c")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _i64 = ctypes.c_int64
+THERMO = {"h": 0, "u": 1, "cv": 2, "cp": 3}
 
 
 def build(force=False):
@@ -99,6 +100,48 @@ class Oracle(_Batch):
         self.dims = tuple(int(x) for x in d)
         self._eval = lambda *a: L.oracle_eval(self.h, *a)
         self._omp = lambda *a: L.oracle_wdot_omp(self.h, *a)
+        L.oracle_dydt_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, _i64, _dp, _dp,
+                                        _i64, _dp]
+        L.oracle_thermo_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, _i64, _dp,
+                                          _i64, _dp]
+        L.oracle_conc_rho_batch.argtypes = [ctypes.c_void_p, _i64, _dp, _dp, _dp,
+                                            _i64, _dp, _dp]
+
+    def dydt(self, p_or_rho, y, conv=False):
+        """dy (N, n) for y (N, n) = [T; Y_0..Y_{N-2}]: constant pressure
+        (p_or_rho = P) or constant volume (p_or_rho = rho)."""
+        p = np.ascontiguousarray(p_or_rho, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        n = p.shape[0]
+        dy = np.zeros((self.dims[0], n))
+        rc = self.lib.oracle_dydt_batch(self.h, int(bool(conv)), n, _ptr(p), _ptr(y), n,
+                                        _ptr(dy))
+        if rc != 0:
+            raise RuntimeError("oracle dydt failed (%d)" % rc)
+        return dy
+
+    def thermo(self, which, T):
+        """which: 'h', 'u', 'cv', 'cp' -> (N, n) at temperatures T."""
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        out = np.zeros((self.dims[0], T.shape[0]))
+        rc = self.lib.oracle_thermo_batch(self.h, THERMO[which], T.shape[0], _ptr(T),
+                                          T.shape[0], _ptr(out))
+        if rc != 0:
+            raise RuntimeError("oracle thermo failed (%d)" % rc)
+        return out
+
+    def conc_rho(self, T, rho, Y):
+        """(misc (3, n): y_N, mw_avg, pres; conc (N, n)) from density."""
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = T.shape[0]
+        misc, conc = np.zeros((3, n)), np.zeros((self.dims[0], n))
+        rc = self.lib.oracle_conc_rho_batch(self.h, n, _ptr(T), _ptr(rho), _ptr(Y), n,
+                                            _ptr(misc), _ptr(conc))
+        if rc != 0:
+            raise RuntimeError("oracle conc_rho failed (%d)" % rc)
+        return misc, conc
 
     def __del__(self):
         try:
@@ -130,6 +173,52 @@ class RefLib(_Batch):
     def available(name, omp=False):
         return os.path.exists(os.path.join(
             HERE, "_ref", name, "libref_omp.so" if omp else "libref.so"))
+
+
+class RefDydt(object):
+    """The reference's emitted dydt (constant pressure) and thermo
+    utilities for one mechanism (oracle/_ref/<name>/libref_dydt.so)."""
+
+    def __init__(self, name):
+        path = os.path.join(HERE, "_ref", name, "libref_dydt.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = L = ctypes.CDLL(path)
+        L.refd_dydt.argtypes = [_i64, _dp, _dp, _i64, _dp]
+        L.refd_thermo.argtypes = [ctypes.c_int, _i64, _dp, _i64, _dp]
+        L.refd_conc_rho.argtypes = [_i64, _dp, _dp, _dp, _i64, _dp, _dp]
+        self.N = RefLib(name).dims[0]
+
+    @staticmethod
+    def available(name):
+        return os.path.exists(os.path.join(HERE, "_ref", name, "libref_dydt.so"))
+
+    def dydt(self, P, y):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        dy = np.zeros((self.N, P.shape[0]))
+        if self.lib.refd_dydt(P.shape[0], _ptr(P), _ptr(y), P.shape[0], _ptr(dy)) != 0:
+            raise RuntimeError("refd_dydt failed")
+        return dy
+
+    def thermo(self, which, T):
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        out = np.zeros((self.N, T.shape[0]))
+        if self.lib.refd_thermo(THERMO[which], T.shape[0], _ptr(T), T.shape[0],
+                                _ptr(out)) != 0:
+            raise RuntimeError("refd_thermo failed")
+        return out
+
+    def conc_rho(self, T, rho, Y):
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = T.shape[0]
+        misc, conc = np.zeros((3, n)), np.zeros((self.N, n))
+        if self.lib.refd_conc_rho(n, _ptr(T), _ptr(rho), _ptr(Y), n, _ptr(misc),
+                                  _ptr(conc)) != 0:
+            raise RuntimeError("refd_conc_rho failed")
+        return misc, conc
 
 
 def gross_scale(blob_tables, fwd, rev, pm):

@@ -4,7 +4,9 @@ For each case below this script writes the mechanism (synthetic, or the
 hand-written features.inp), has the reference's own generator emit C for it
 (oracle/build_ref.py: a Python 3-patched copy of the reference in a scratch
 directory), compiles that C with -O2 -ffp-contract=off and evaluates it on
-seeded states plus edge states.  The outputs of every stage are stored as
+seeded states plus edge states: every stage of the rates path, the thermo
+utilities (eval_h/u/cv/cp, eval_conc_rho) and the constant-pressure dydt
+(compiled with -DCONP).  The outputs are stored as
 <case>.npz together with the mechanism text, so that the tests can pin the
 front end and the oracle without the reference checkout.
 
@@ -24,7 +26,7 @@ sys.path.insert(0, REPO)
 
 from create_rate_subs_gb300 import chem, synth  # noqa: E402
 from oracle import build_ref  # noqa: E402
-from oracle.oracle import RefLib  # noqa: E402
+from oracle.oracle import RefDydt, RefLib  # noqa: E402
 
 # case -> (mechanism source, last_spec, n random states, state seed)
 CASES = {
@@ -108,6 +110,14 @@ def make_case(case):
     P = np.concatenate([P, Pe])
     Y = np.concatenate([Y, Ye], axis=1)
     out = ref.eval(T, P, Y)
+    # the emitted thermo utilities and constant-pressure dydt on the same
+    # states (y = [T, Y_0..Y_{N-2}]); eval_conc_rho at the density that
+    # eval_conc returned
+    refd = RefDydt(name)
+    for w in ("h", "u", "cv", "cp"):
+        out["thermo_" + w] = refd.thermo(w, T)
+    out["conc_rho_misc"], out["conc_rho"] = refd.conc_rho(T, out["misc"][2], Y)
+    out["dydt_conp"] = refd.dydt(P, np.concatenate([T[None], Y[: N - 1]], axis=0))
     with open(mp) as f:
         mech_text = f.read()
     with open(tp) as f:
