@@ -312,6 +312,28 @@ def run_ours(args):
                  "speedup_vs_plain": ms_plain22 / msm, "error_vs_fp64": accuracy["mixed"]}
         del mT, mP, mY, mo
 
+    # the ODE right-hand side around wdot (dydt, rate_subs.py:1829-2067)
+    ydy = torch.cat([dT[None], dY], dim=0)
+    dyo = torch.empty_like(ydy)
+    rho = torch.empty_like(dT)
+    # the density of each state, for the constant-volume form
+    _lib.check(lib.crs_eval_conc_batch(rs.h, n, ctypes.c_void_p(dT.data_ptr()),
+                                       ctypes.c_void_p(dP.data_ptr()),
+                                       ctypes.c_void_p(dY.data_ptr()), n, None, None,
+                                       ctypes.c_void_p(rho.data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr()),
+                                       ctypes.c_void_p(stream.cuda_stream)))
+    dydt_res = {}
+    for form, arg, conv in (("conp", dP, False), ("conv", rho, True)):
+        for m in (plain, "mixed"):
+            if m not in modes:
+                continue
+            msd = _time_steps(lambda: rs.dydt(arg, ydy, conv=conv, mode=m, out=dyo),
+                              max(2, args.steps // 2), 1, stream, dist)
+            dydt_res["%s_%s" % (form, m)] = {"value": n * world / (msd * 1e-3),
+                                             "unit": "states/s", "ms_per_step": msd}
+    del ydy, dyo, rho
+
     # end to end through the C ABI with host buffers: crs_wdot_host copies
     # the pinned inputs in, evaluates and copies wdot out (chunks on two
     # streams, copies overlapping kernels); host clock around whole calls
@@ -371,6 +393,7 @@ def run_ours(args):
         "modes_states_per_s": per_mode,
         "accuracy_vs_fp64_strict": accuracy,
         "mixed": mixed,
+        "dydt": dydt_res,
         "e2e": {"value": n * world / (ms_e2e * 1e-3), "unit": "states/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e, "matches_device_result": e2e_ok,

@@ -149,7 +149,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   L.NREV = (int)dims[2];
   L.NPM = (int)dims[3];
   L.NRATE = (int)dims[4];
-  if (L.N < 2 || L.R < 0 || L.NREV < 0 || L.NPM < 0 || L.NRATE < L.R)
+  if (L.N < 2 || L.N > 32767 || L.R < 0 || L.NREV < 0 || L.NPM < 0 || L.NRATE < L.R)
     return fail(CRS_ERR_BLOB, "bad dims");
   // Sections the fast kernels read come first; the ones only the
   // reference-order kernels read (per-reaction Kc polynomials, raw NASA-7
@@ -269,28 +269,32 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       if (d.field == f) secs.emplace_back(f, d.bytes);
   };
   using IL = crs::ImgLayout;
-  // Region order T F S M K D (see ImgLayout::rng):
+  // Region order T F S2 S1 M K D (see ImgLayout::rng):
   // [T] one-state-per-thread tables
   der(&IL::perm); der(&IL::seg); der(&IL::rfac); der(&IL::pfac);
   const size_t iF = secs.size();
   // [F] FP64 only
   der(&IL::exptab); der(&IL::rate_x);
   const size_t iS = secs.size();
-  // [S] shared by the fast kernels
-  der(&IL::kc_lpref); der(&IL::sp_gibbs);
-  raw(&IL::sp_tmid, "sp_tmid"); raw(&IL::inv_mw, "sp_inv_mw");
+  // [S2] shared by the fast kernels except the mixed one-state-per-thread
+  // kernel (Gibbs terms, generic reactant / product lists)
+  der(&IL::sp_gibbs); raw(&IL::sp_tmid, "sp_tmid");
   raw(&IL::rate_kind, "rate_kind"); raw(&IL::rx_ptr, "rx_ptr");
   raw(&IL::rx_sp, "rx_sp"); raw(&IL::rx_nint, "rx_nint");
   raw(&IL::px_ptr, "px_ptr"); raw(&IL::px_sp, "px_sp");
-  raw(&IL::px_nint, "px_nint"); raw(&IL::rev_idx, "rev_idx");
-  raw(&IL::pm_idx, "pm_idx"); raw(&IL::nu_ptr, "nu_ptr");
-  raw(&IL::nu_sp, "nu_sp"); raw(&IL::nu_val, "nu_val");
+  raw(&IL::px_nint, "px_nint");
+  const size_t iS1 = secs.size();
+  // [S1] shared by all fast kernels
+  raw(&IL::inv_mw, "sp_inv_mw");
+  raw(&IL::rev_idx, "rev_idx"); raw(&IL::pm_idx, "pm_idx");
+  raw(&IL::nu_ptr, "nu_ptr"); raw(&IL::nu_sp, "nu_sp"); raw(&IL::nu_val, "nu_val");
   const size_t iM = secs.size();
   // [M] mixed only
   der(&IL::rate_ff); der(&IL::inv_mw_f);
   const size_t iK = secs.size();
-  // [K] per-reaction Kc polynomials (mixed, one state per thread)
-  der(&IL::kc_poly);
+  // [K] per-reaction Kc polynomials (mixed, one state per thread) and the
+  // ln Kc prefactors (read through L1 by the Gibbs-column layouts)
+  der(&IL::kc_poly); der(&IL::kc_lpref);
   raw(&IL::kc_ptr, "kc_ptr"); raw(&IL::kc_tmid, "kc_tmid");
   raw(&IL::kc_lo, "kc_lo"); raw(&IL::kc_hi, "kc_hi");
   const size_t iD = secs.size();
@@ -336,13 +340,13 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   out.resize((out.size() + 15) / 16 * 16);
   L2.bytes = (int)out.size();
   starts.push_back((int)out.size());
-  const int T0 = starts[0], F0 = starts[iF], S0 = starts[iS], M0 = starts[iM],
-            K0 = starts[iK], D0 = starts[iD], C0 = starts[iC];
-  const int rng[5][4] = {{T0, M0, 0, 0},    // FP64 per thread: T F S
-                         {F0, M0, D0, C0},  // FP64 per warp: F S + D
-                         {T0, F0, S0, K0},  // mixed per thread: T + S M
-                         {S0, K0, D0, C0},  // mixed per warp: S M + D
-                         {T0, F0, S0, D0}}; // mixed per thread: T + S M K
+  const int T0 = starts[0], F0 = starts[iF], S0 = starts[iS], S1 = starts[iS1],
+            M0 = starts[iM], K0 = starts[iK], D0 = starts[iD], C0 = starts[iC];
+  const int rng[5][4] = {{T0, M0, 0, 0},    // FP64 per thread: T F S2 S1
+                         {F0, M0, D0, C0},  // FP64 per warp: F S2 S1 + D
+                         {T0, F0, S1, K0},  // mixed per thread: T + S1 M
+                         {S0, K0, D0, C0},  // mixed per warp: S2 S1 M + D
+                         {T0, F0, S1, D0}}; // mixed per thread: T + S1 M K
   memcpy(L2.rng, rng, sizeof rng);
   img.swap(out);
   L = L2;

@@ -23,6 +23,8 @@
 #include <cstring>
 #include <vector>
 
+#include <type_traits>
+
 #include "crs_internal.cuh"
 #include "crs_shapes.cuh"
 
@@ -178,22 +180,25 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   put(extra, &ImgLayout::sri_ff, sf);
   put(extra, &ImgLayout::eff_f, ef);
   // reaction order for the shape-specialised paths and expanded factors
-  std::vector<int32_t> rfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0),
-      pfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0), shape(L.R, NSHAPE);
+  // species indices as int16 (the mechanism is checked to have fewer than
+  // 32768 species): half the shared memory of int32
+  std::vector<int16_t> rfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0),
+      pfac((size_t)MAXF * (L.R > 0 ? L.R : 1), 0);
+  std::vector<int32_t> shape(L.R, NSHAPE);
   for (int r = 0; r < L.R; ++r) {
     bool ok = t.rate_kind[r] == RATE_EXP && t.pm_idx[r] < 0;
     int nr = 0, np = 0;
     for (int q = t.rx_ptr[r]; q < t.rx_ptr[r + 1]; ++q) {
       if (t.rx_nint[q] < 0) ok = false;
       for (int c = 0; c < t.rx_nint[q] && ok; ++c) {
-        if (nr < MAXF) rfac[(size_t)MAXF * r + nr] = t.rx_sp[q];
+        if (nr < MAXF) rfac[(size_t)MAXF * r + nr] = (int16_t)t.rx_sp[q];
         ++nr;
       }
     }
     for (int q = t.px_ptr[r]; q < t.px_ptr[r + 1]; ++q) {
       if (t.px_nint[q] < 0) ok = false;
       for (int c = 0; c < t.px_nint[q] && ok; ++c) {
-        if (np < MAXF) pfac[(size_t)MAXF * r + np] = t.px_sp[q];
+        if (np < MAXF) pfac[(size_t)MAXF * r + np] = (int16_t)t.px_sp[q];
         ++np;
       }
     }
@@ -310,9 +315,11 @@ __device__ __forceinline__ double exp_core(double x, const double *tab) {
                                     __double2loint(tj));
   return fma(s, p, s);
 }
-// Overflow, underflow and NaN go to CUDA's exp.
+// Overflow, underflow and NaN go to CUDA's exp.  |x| <= 700 is tested on
+// the high word as an integer (0x4085E000 = high word of 700.0; a larger
+// low word still leaves x below 700.0001): no FP64 instruction.
 __device__ __forceinline__ double exp_fix(double x, double e) {
-  return (fabs(x) <= 700.0) ? e : exp(x);
+  return ((unsigned)__double2hiint(x) & 0x7fffffffu) <= 0x4085E000u ? e : exp(x);
 }
 __device__ __forceinline__ double exp_t(double x, const double *tab) {
   return exp_fix(x, exp_core(x, tab));
@@ -329,6 +336,22 @@ struct Arr {
   double *p;
   __device__ double &operator[](int k) const { return p[k]; }
 };
+
+// Kc exponent from the per-species Gibbs column S: ln(prefactor) +
+// sum_k nu_k S_k (the layouts that keep S on chip).
+template <class CS>
+struct KcCol {
+  CS S;
+  __device__ __forceinline__ double operator()(const Tab &t, int r, int j) const {
+    double g = t.kc_lpref[j];
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) g = fma(t.nu_val[e], S[t.nu_sp[e]], g);
+    return g;
+  }
+};
+template <class T>
+struct IsKcCol { static constexpr bool value = false; };
+template <class CS>
+struct IsKcCol<KcCol<CS>> { static constexpr bool value = true; };
 
 struct State {
   double T, invT, logT;
@@ -420,13 +443,29 @@ __device__ double pres_mod(const Tab &t, int p, const State &s, double mix,
   return low ? F * Pr * inv1p : F * inv1p;
 }
 
+// wdot[k] += nu * net for the reactions of one block, in order.
+template <int NNU, class DC>
+__device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
+                                           const double (&net)[4], const DC &W) {
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (u >= cnt) break;
+    const int e0 = t.nu_ptr[rr[u]];
+#pragma unroll
+    for (int q = 0; q < NNU; ++q) {
+      const int k = t.nu_sp[e0 + q];
+      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);
+    }
+  }
+}
+
 // Four reactions of one shape (crs_shapes.cuh): rate constants, products
 // and net rates with compile-time trip counts, so that the four dependency
 // chains interleave; then their wdot contributions in order.
-template <int NR, int NP, int NNU, int REV, bool STAGES>
+template <int NR, int NP, int NNU, int REV, bool STAGES, class KC>
 __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
                                             int cnt, const State &s,
-                                            const Col &C, const Col &S,
+                                            const Col &C, const KC &kc,
                                             const Col &W, const Batch &b,
                                             int64_t i) {
   double net[4], x[4], e[4];
@@ -446,10 +485,15 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
     fwd[u] = f;
     rev[u] = 0.0;
     if (REV) {
-      const int e0 = t.nu_ptr[r];
-      double g = t.kc_lpref[t.rev_idx[r]];
+      double g;
+      if constexpr (IsKcCol<KC>::value) {
+        const int e0 = t.nu_ptr[r];
+        g = t.kc_lpref[t.rev_idx[r]];
 #pragma unroll
-      for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], S[t.nu_sp[e0 + q]], g);
+        for (int q = 0; q < NNU; ++q) g = fma(t.nu_val[e0 + q], kc.S[t.nu_sp[e0 + q]], g);
+      } else {
+        g = kc(t, r, t.rev_idx[r]);
+      }
       x[u] = x[u] - g;
       e[u] = exp_core(x[u], s.tab);
     }
@@ -466,26 +510,20 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u) net[u] = fwd[u] - rev[u];
+  if (STAGES) {
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    if (u >= cnt) break;
-    const int r = rr[u];
-    if (STAGES) {
-      if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd[u];
-      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[r] * b.ld + i] = rev[u];
-    }
-    const int e0 = t.nu_ptr[r];
-#pragma unroll
-    for (int q = 0; q < NNU; ++q) {
-      const int k = t.nu_sp[e0 + q];
-      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);
+    for (int u = 0; u < 4; ++u) {
+      if (u >= cnt) break;
+      if (b.fwd) b.fwd[(int64_t)rr[u] * b.ld + i] = fwd[u];
+      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[rr[u]] * b.ld + i] = rev[u];
     }
   }
+  accumulate<NNU>(t, rr, cnt, net, W);
 }
 
-template <int SH, bool STAGES>
+template <int SH, bool STAGES, class KC>
 __device__ __forceinline__ void run_shape(const Tab &t, const State &s,
-                                          const Col &C, const Col &S,
+                                          const Col &C, const KC &S,
                                           const Col &W, const Batch &b,
                                           int64_t i) {
   constexpr Shape d = shape_of(SH);
@@ -499,29 +537,29 @@ __device__ __forceinline__ void run_shape(const Tab &t, const State &s,
   }
 }
 
-template <int SH, bool STAGES>
+template <int SH, bool STAGES, class KC>
 struct Shapes {
   __device__ __forceinline__ static void run(const Tab &t, const State &s,
-                                             const Col &C, const Col &S,
+                                             const Col &C, const KC &S,
                                              const Col &W, const Batch &b,
                                              int64_t i) {
     run_shape<SH, STAGES>(t, s, C, S, W, b, i);
-    Shapes<SH + 1, STAGES>::run(t, s, C, S, W, b, i);
+    Shapes<SH + 1, STAGES, KC>::run(t, s, C, S, W, b, i);
   }
 };
-template <bool STAGES>
-struct Shapes<NSHAPE, STAGES> {
+template <bool STAGES, class KC>
+struct Shapes<NSHAPE, STAGES, KC> {
   __device__ __forceinline__ static void run(const Tab &, const State &,
-                                             const Col &, const Col &,
+                                             const Col &, const KC &,
                                              const Col &, const Batch &,
                                              int64_t) {}
 };
 
 // Net rate (fwd - rev) * pres_mod of any reaction: general rate forms,
 // pressure modification, non-integer coefficients.
-template <class CS>
+template <class CS, class KC>
 __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
-                                          double mix, const CS &C, const CS &S,
+                                          double mix, const CS &C, const KC &kc,
                                           double &fwd, double &rev, double &pm) {
   double xf = 0.0;
   const double kf = rate(t, r, s, xf);
@@ -530,9 +568,7 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   double net = fwd;
   rev = 0.0;
   if (j >= 0) {
-    double gsum = t.kc_lpref[j];
-    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e)
-      gsum = fma(t.nu_val[e], S[t.nu_sp[e]], gsum);
+    const double gsum = kc(t, r, j);
     const double kr = (t.rate_kind[r] == RATE_EXP) ? exp_t(xf - gsum, s.tab)
                                                    : kf * exp_t(-gsum, s.tab);
     rev = kr * product(t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r], t.px_ptr[r + 1], C);
@@ -547,10 +583,10 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   return net;
 }
 
-template <bool STAGES>
+template <bool STAGES, class KC>
 __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
                                         double mix, const Col &C,
-                                        const Col &S, const Col &W,
+                                        const KC &S, const Col &W,
                                         const Batch &b, int64_t i) {
   double fwd, rev, pm;
   const double net = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
@@ -566,8 +602,12 @@ __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
   }
 }
 
-template <bool STAGES>
-__global__ void __launch_bounds__(128, 1)
+// KCM 0: Kc from a per-species Gibbs column S (3 columns of 8 B per
+// species and thread); 1 / 2: from the per-reaction Kc polynomials (single /
+// several T_common groups; 2 columns, so more threads fit next to the
+// tables).
+template <bool STAGES, int KCM>
+__global__ void __launch_bounds__(256, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
@@ -579,7 +619,7 @@ __global__ void __launch_bounds__(128, 1)
   const int64_t st = blockDim.x;
   const Col C{base + threadIdx.x, st};
   const Col W{base + (int64_t)N * st + threadIdx.x, st};
-  const Col S{base + (int64_t)2 * N * st + threadIdx.x, st};
+  const Col S{base + (int64_t)2 * N * st + threadIdx.x, st};  // KCM 0 only
   int bad = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -602,24 +642,42 @@ __global__ void __launch_bounds__(128, 1)
     const double rho = P / mwi * (s.invT * INV_RU);
     for (int k = 0; k < N - 1; ++k) C[k] = C[k] * (rho * t.inv_mw[k]);
     C[N - 1] = yN * (rho * t.inv_mw[N - 1]);
-    // per-species Gibbs terms and accumulators
+    const long long Tbits = __double_as_longlong(s.T);
     for (int k = 0; k < N; ++k) {
-      const double *g = t.sp_gibbs + 14 * k + ((s.T <= t.sp_tmid[k]) ? 0 : 7);
-      const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
-      double v = fma(h, s.T, g[0]);
-      v = fma(g[1], s.logT, v);
-      S[k] = fma(g[6], s.invT, v);
+      if (KCM == 0) {
+        // per-species Gibbs terms (T <= T_common on the positive doubles'
+        // bit patterns)
+        const double *g = t.sp_gibbs + 14 * k +
+                          ((Tbits <= __double_as_longlong(t.sp_tmid[k])) ? 0 : 7);
+        const double h = fma(fma(fma(g[5], s.T, g[4]), s.T, g[3]), s.T, g[2]);
+        double v = fma(h, s.T, g[0]);
+        v = fma(g[1], s.logT, v);
+        S[k] = fma(g[6], s.invT, v);
+      }
       W[k] = 0.0;
     }
     if (STAGES && b.conc)
       for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = C[k];
     const double mix = P * s.invT * INV_RU;
-    Shapes<0, STAGES>::run(t, s, C, S, W, b, i);
-    for (int p = t.seg[NSHAPE]; p < t.R; ++p)
-      general<STAGES>(t, t.perm[p], s, mix, C, S, W, b, i);
+    if constexpr (KCM == 0) {
+      const KcCol<Col> kc{S};
+      Shapes<0, STAGES, KcCol<Col>>::run(t, s, C, kc, W, b, i);
+      for (int p = t.seg[NSHAPE]; p < t.R; ++p)
+        general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
+    } else {
+      using KC = typename std::conditional<KCM == 1, KcPoly1, KcPolyG>::type;
+      KC kc;
+      kc.T = s.T;
+      kc.logT = s.logT;
+      kc.invT = s.invT;
+      if constexpr (KCM == 1) kc.Tbits = Tbits;
+      Shapes<0, STAGES, KC>::run(t, s, C, kc, W, b, i);
+      for (int p = t.seg[NSHAPE]; p < t.R; ++p)
+        general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
+    }
     for (int k = 0; k < N; ++k) {
       const double v = W[k];
-      bad += !isfinite(v);
+      bad += ((__double2hiint(v) >> 20) & 0x7ff) == 0x7ff;  // inf or NaN, integer test
       b.wdot[(int64_t)k * b.ld + i] = v;
     }
   }
@@ -717,7 +775,7 @@ __global__ void __launch_bounds__(DW * 32)
       for (int p = lane; p < R; p += 32) {
         const int r = t.dperm[p];
         double fwd, rev, pm;
-        q[r] = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+        q[r] = rxn_net(t, r, s, mix, C, KcCol<Arr>{S}, fwd, rev, pm);
         if (STAGES) {
           const int jr = t.rev_idx[r], pp = t.pm_idx[r];
           if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
@@ -749,12 +807,23 @@ int grid_for(int64_t n, int block, int max_ctas);
 cudaError_t launch_wdot_fp64_tps(const unsigned char *img, const ImgLayout &L,
                                  const Batch &b, int sm_count, int smem_optin,
                                  cudaStream_t s) {
-  const int block = 128;
   const size_t tab = (size_t)(L.rng[0][1] - L.rng[0][0] + L.rng[0][3] - L.rng[0][2]);
-  const size_t bytes = tab + (size_t)3 * L.N * block * sizeof(double);
-  if (bytes > (size_t)smem_optin) return cudaErrorNotSupported;
+  auto fit = [&](int cols) {
+    const long long room = (long long)smem_optin - (long long)tab;
+    int nt = room > 0 ? (int)(room / ((long long)cols * L.N * 8)) / 32 * 32 : 0;
+    return nt > 256 ? 256 : nt;
+  };
+  // the polynomial layout when it buys more threads than the Gibbs column
+  const int nt2 = fit(2), nt3 = fit(3);
+  const int kcm = (nt2 > nt3 && nt2 >= 64) ? (L.kc_single ? 1 : 2) : 0;
+  const int block = kcm ? nt2 : nt3;
+  if (block < 32) return cudaErrorNotSupported;
+  const size_t bytes = tab + (size_t)(kcm ? 2 : 3) * L.N * block * sizeof(double);
   const bool stages = b.conc || b.fwd || b.rev || b.pm;
-  auto k = stages ? fast::k_wdot<true> : fast::k_wdot<false>;
+  void (*k)(const unsigned char *, ImgLayout, Batch);
+  if (kcm == 0) k = stages ? fast::k_wdot<true, 0> : fast::k_wdot<false, 0>;
+  else if (kcm == 1) k = stages ? fast::k_wdot<true, 1> : fast::k_wdot<false, 1>;
+  else k = stages ? fast::k_wdot<true, 2> : fast::k_wdot<false, 2>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
   return cudaGetLastError();

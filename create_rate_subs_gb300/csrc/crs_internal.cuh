@@ -66,7 +66,8 @@ struct ImgLayout {
 
 // Typed view of an image (in shared or global memory).
 struct Tab {
-  const int32_t *perm, *seg, *rfac, *pfac;
+  const int32_t *perm, *seg;
+  const int16_t *rfac, *pfac;
   const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
   const double *spc_nu;
   const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
@@ -99,7 +100,9 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
 #define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
   CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
   CRS_F(exptab); CRS_F(kc_poly); CRS_F(sp_thermo);
-  CRS_I(perm); CRS_I(seg); CRS_I(rfac); CRS_I(pfac);
+  CRS_I(perm); CRS_I(seg);
+  t.rfac = reinterpret_cast<const int16_t *>(CRS_P(rfac));
+  t.pfac = reinterpret_cast<const int16_t *>(CRS_P(pfac));
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
   CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
@@ -258,6 +261,46 @@ cudaError_t launch_conc_rho(const unsigned char *img, const ImgLayout &L, int64_
 cudaError_t launch_dydt_finish(const unsigned char *img, const ImgLayout &L, int conv,
                                int64_t n, const double *y, int64_t ld, const double *p_or_rho,
                                const double *W, double *dy, int sm_count, cudaStream_t s);
+
+#ifdef __CUDACC__
+// Exponent of the equilibrium constant of reversible reaction j (with ln
+// of its prefactor) from the reaction's own polynomial in T, summed over
+// its T_common groups (rate_subs.py:592-655 forms these coefficients):
+// c0 + c1 ln T + T (c2 + T (c3 + T (c4 + c5 T))) - c6 / T, in FP64.  Needs
+// no per-state column.  KcPoly1: one group per reaction (kc_poly), the
+// prefactor folded into c0 and the T <= T_common test made on the positive
+// doubles' bit patterns as integers, so that only the polynomial's six
+// FMAs use the FP64 pipe and the code has no branch.
+struct KcPoly1 {
+  double T, logT, invT;
+  long long Tbits;
+  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
+    const double *p = t.kc_poly + 16 * j;
+    const double *c = (Tbits <= __double_as_longlong(p[0])) ? p + 2 : p + 9;
+    double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
+    h = fma(h, T, c[0]);
+    h = fma(c[1], logT, h);
+    return fma(-c[6], invT, h);
+  }
+};
+
+// Several T_common groups in a reaction: sum the groups' polynomials.
+struct KcPolyG {
+  double T, logT, invT;
+  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
+    double g = t.kc_lpref[j];
+    for (int q = t.kc_ptr[j]; q < t.kc_ptr[j + 1]; ++q) {
+      const double *c = (T <= t.kc_tmid[q]) ? t.kc_lo + 7 * q : t.kc_hi + 7 * q;
+      double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
+      h = fma(h, T, c[0]);
+      h = fma(c[1], logT, h);
+      g += fma(-c[6], invT, h);
+    }
+    return g;
+  }
+};
+
+#endif
 
 // Sets the text returned by crs_last_error() and returns code.
 int report(int code, const char *msg);

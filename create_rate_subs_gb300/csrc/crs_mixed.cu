@@ -235,42 +235,6 @@ struct KcFromGibbs {
   }
 };
 
-// The same exponent from the reaction's own polynomial in T, summed over
-// its T_common groups (rate_subs.py:592-655 forms these coefficients):
-// c0 + c1 ln T + T (c2 + T (c3 + T (c4 + c5 T))) - c6 / T, in FP64.  Needs
-// no per-state column.  KcPoly1: one group per reaction (kc_poly), the
-// prefactor folded into c0 and the T <= T_common test made on the positive
-// doubles' bit patterns as integers, so that only the polynomial's six
-// FMAs use the FP64 pipe and the code has no branch.
-struct KcPoly1 {
-  double T, logT, invT;
-  long long Tbits;
-  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
-    const double *p = t.kc_poly + 16 * j;
-    const double *c = (Tbits <= __double_as_longlong(p[0])) ? p + 2 : p + 9;
-    double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
-    h = fma(h, T, c[0]);
-    h = fma(c[1], logT, h);
-    return fma(-c[6], invT, h);
-  }
-};
-
-// Several T_common groups in a reaction: sum the groups' polynomials.
-struct KcPolyG {
-  double T, logT, invT;
-  __device__ __forceinline__ double operator()(const Tab &t, int, int j) const {
-    double g = t.kc_lpref[j];
-    for (int q = t.kc_ptr[j]; q < t.kc_ptr[j + 1]; ++q) {
-      const double *c = (T <= t.kc_tmid[q]) ? t.kc_lo + 7 * q : t.kc_hi + 7 * q;
-      double h = fma(fma(fma(c[5], T, c[4]), T, c[3]), T, c[2]);
-      h = fma(h, T, c[0]);
-      h = fma(c[1], logT, h);
-      g += fma(-c[6], invT, h);
-    }
-    return g;
-  }
-};
-
 // product of concentration factors as mantissa * 2^E
 // Product of concentration factors, times the mantissa m0 of the rate
 // constant, as mantissa * 2^E; the FP32 rounding of every multiply is kept
@@ -388,6 +352,22 @@ __device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
   return low ? F * frac : F * inv1p;
 }
 
+// wdot[k] += nu * net (FP64) for the reactions of one block, in order.
+template <int NNU, class DC>
+__device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
+                                           const double (&net)[4], const DC &W) {
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (u >= cnt) break;
+    const int e0 = t.nu_ptr[rr[u]];
+#pragma unroll
+    for (int q = 0; q < NNU; ++q) {
+      const int k = t.nu_sp[e0 + q];
+      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);  // FP64 accumulation
+    }
+  }
+}
+
 template <int NR, int NP, int NNU, int REV, bool STAGES, class KC>
 __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
                                             int cnt, const State &s,
@@ -441,22 +421,18 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
       rev[u] = assemble(m + err, E);
     }
   }
+  double net[4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    if (u >= cnt) break;
-    const int r = rr[u];
-    const double net = fwd[u] - rev[u];  // FP64
-    if (STAGES) {
-      if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd[u];
-      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[r] * b.ld + i] = rev[u];
-    }
-    const int e0 = t.nu_ptr[r];
+  for (int u = 0; u < 4; ++u) net[u] = fwd[u] - rev[u];  // FP64
+  if (STAGES) {
 #pragma unroll
-    for (int q = 0; q < NNU; ++q) {
-      const int k = t.nu_sp[e0 + q];
-      W[k] = fma(t.nu_val[e0 + q], net, W[k]);  // FP64 accumulation
+    for (int u = 0; u < 4; ++u) {
+      if (u >= cnt) break;
+      if (b.fwd) b.fwd[(int64_t)rr[u] * b.ld + i] = fwd[u];
+      if (REV && b.rev) b.rev[(int64_t)t.rev_idx[rr[u]] * b.ld + i] = rev[u];
     }
   }
+  accumulate<NNU>(t, rr, cnt, net, W);
 }
 
 template <int SH, bool STAGES, class KC>
@@ -542,10 +518,11 @@ __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
 // One state per thread.  Per-state shared-memory columns: C (fp32) and
 // the wdot accumulators W (FP64), 12 B per species and thread; the Kc
 // exponents come from the per-reaction polynomials (no Gibbs column, the
-// polynomials read through L1), so that 256 threads fit next to the
-// staged tables.  KC1: one T_common group per reaction (kc_poly).
+// polynomials read through L1), and only the tables of this kernel's hot
+// loop are staged, so that ~300 threads fit.  KC1: one T_common group per
+// reaction (kc_poly).
 template <bool STAGES, bool KC1>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(352, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
@@ -771,16 +748,17 @@ __global__ void __launch_bounds__(DW * 32)
 int grid_for(int64_t n, int block, int max_ctas);
 
 // Thread-per-state mixed kernel (CRS_MODE_MIXED_TPS, and CRS_MODE_MIXED
-// when it fits): as many threads per CTA (multiple of 32, at most 256) as
-// the shared memory left by the tables allows.
+// when it fits): as many threads per CTA (at most 352) as the shared
+// memory left by the tables allows.
 cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
                                   const Batch &b, int sm_count, int smem_optin,
                                   cudaStream_t s) {
   const size_t tab = (size_t)(L.rng[2][1] - L.rng[2][0] + L.rng[2][3] - L.rng[2][2]);
   const size_t per = (size_t)L.N * (8 + 4);
   const long long room = (long long)smem_optin - (long long)tab;
-  int block = room > 0 ? (int)(room / (long long)per) / 32 * 32 : 0;
-  if (block > 256) block = 256;
+  // any thread count: a last partial warp still adds states in flight
+  int block = room > 0 ? (int)(room / (long long)per) : 0;
+  if (block > 352) block = 352;
   if (block < 32) return cudaErrorNotSupported;
   const size_t bytes = tab + per * block;
   const bool stages = b.conc || b.fwd || b.rev || b.pm;
