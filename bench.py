@@ -505,6 +505,15 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     err_raw = q(e_raw)
     served = (w == raw).all(dim=0)          # states the network answered
     err_served = q(e_raw[served])
+    # the gate's trade-off: tighter residual tolerances send more states to
+    # the exact kernel
+    sweep = []
+    for tl in (0.05, 0.01, 0.003, 0.001, 0.0003):
+        mst = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tl, out=out), 2, 1, stream, dist)
+        wt, nf = sur.wdot(Te, Pe, Ye, tol=tl, out=out)
+        et = q(((wt - exact).abs() / den).amax(dim=0))
+        sweep.append({"tol": tl, "fallback_fraction": nf / ne,
+                      "states_per_s": ne * world / (mst * 1e-3), "error": et})
     peak = None
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -533,12 +542,13 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
                             "s_k = std of wdot_k over the training states",
         "error_gated": err_gated, "error_network_all_states": err_raw,
         "error_network_served_states": err_served,
+        "gate_sweep": sweep,
         "roofline": {"bound": "tensor", "kernel": "network forward (4 tcgen05 GEMMs + "
                      "epilogues)", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
                      "frac": fwd_tflops / peak, "flops_per_state": 2 * macs,
                      "peak_note": "bf16 burst, of measured"},
     }
-    del Te, Pe, Ye, out, exact, w, raw, den, e_raw, served
+    del Te, Pe, Ye, out, exact, w, raw, den, e_raw, served, wt
     return res
 
 
