@@ -176,6 +176,12 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
       {"kc_tmid", &L.kc_tmid, 1}, {"kc_lo", &L.kc_lo, 1},
       {"kc_hi", &L.kc_hi, 1}, {"sp_lo", &L.sp_lo, 1},
       {"sp_hi", &L.sp_hi, 1}, {"sp_mw", &L.sp_mw, 1},
+      {"rate_aux", &L.rate_aux, 2}, {"plog_ptr", &L.plog_ptr, 2},
+      {"plog_row", &L.plog_row, 2}, {"plog_p", &L.plog_p, 1},
+      {"plog_lp", &L.plog_lp, 1}, {"plog_dlp", &L.plog_dlp, 1},
+      {"cheb_ptr", &L.cheb_ptr, 2}, {"cheb_nt", &L.cheb_nt, 2},
+      {"cheb_np", &L.cheb_np, 2}, {"cheb_par", &L.cheb_par, 1},
+      {"cheb_tp", &L.cheb_tp, 1},
   };
   std::vector<unsigned char> &img = m->h_img;
   img.clear();
@@ -234,9 +240,35 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   for (int r = 0; r < L.R; ++r) {
     if (t.rev_idx[r] >= 0 && t.rev_idx[r] != nrev++) return fail(CRS_ERR_BLOB, "bad rev_idx");
     if (t.pm_idx[r] >= 0 && t.pm_idx[r] != npm++) return fail(CRS_ERR_BLOB, "bad pm_idx");
-    if (!in(t.rate_kind[r], 0, 4) || t.rate_npow[r] > 64) return fail(CRS_ERR_BLOB, "bad rate");
+    if (!in(t.rate_kind[r], 0, 6) || t.rate_npow[r] > 64) return fail(CRS_ERR_BLOB, "bad rate");
   }
   if (nrev != L.NREV || npm != L.NPM) return fail(CRS_ERR_BLOB, "rev/pm counts disagree");
+  // PLOG / Chebyshev rows: indices in range, PLOG points plain Arrhenius rows
+  const int64_t nplog = cnt("plog_ptr") - 1, ncheb = cnt("cheb_nt");
+  if (cnt("rate_aux") != L.NRATE || nplog < 0 || cnt("cheb_ptr") != ncheb + 1 ||
+      cnt("cheb_np") != ncheb || cnt("cheb_tp") != 4 * ncheb ||
+      cnt("plog_row") != cnt("plog_p") || cnt("plog_lp") != cnt("plog_p") ||
+      cnt("plog_dlp") != cnt("plog_p"))
+    return fail(CRS_ERR_BLOB, "PLOG/Chebyshev table sizes disagree");
+  if (!ptr_ok(t.plog_ptr, (int)nplog, cnt("plog_p")) || !ptr_ok(t.cheb_ptr, (int)ncheb, cnt("cheb_par")))
+    return fail(CRS_ERR_BLOB, "bad PLOG/Chebyshev pointers");
+  for (int64_t q = 0; q < nplog; ++q)
+    if (t.plog_ptr[q + 1] - t.plog_ptr[q] < 1) return fail(CRS_ERR_BLOB, "empty PLOG entry");
+  for (int64_t e = 0; e < cnt("plog_row"); ++e)
+    if (!in(t.plog_row[e], 0, L.NRATE) || t.rate_kind[t.plog_row[e]] > crs::RATE_POW)
+      return fail(CRS_ERR_BLOB, "bad PLOG rate row");
+  for (int64_t q = 0; q < ncheb; ++q)
+    if (t.cheb_nt[q] < 2 || t.cheb_nt[q] > crs::CHEB_MAX || t.cheb_np[q] < 2 ||
+        (int64_t)t.cheb_nt[q] * t.cheb_np[q] != t.cheb_ptr[q + 1] - t.cheb_ptr[q])
+      return fail(CRS_ERR_BLOB, "bad Chebyshev block");
+  for (int r = 0; r < L.NRATE; ++r) {
+    const int k = t.rate_kind[r];
+    if (!in(k, 0, 6)) return fail(CRS_ERR_BLOB, "bad rate kind");
+    if (k == crs::RATE_PLOG && !in(t.rate_aux[r], 0, nplog)) return fail(CRS_ERR_BLOB, "bad PLOG index");
+    if (k == crs::RATE_CHEB && !in(t.rate_aux[r], 0, ncheb)) return fail(CRS_ERR_BLOB, "bad Chebyshev index");
+    if ((k == crs::RATE_PLOG || k == crs::RATE_CHEB) && r >= L.R)
+      return fail(CRS_ERR_BLOB, "PLOG/Chebyshev only as reaction rows");
+  }
   for (int p = 0; p < L.NPM; ++p) {
     if (!in(t.pm_kind[p], 0, 3) || !in(t.pm_form[p], 0, 3) || t.pm_sp[p] >= L.N)
       return fail(CRS_ERR_BLOB, "bad pres_mod entry");
@@ -316,6 +348,10 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   raw(&IL::pm_troe, "pm_troe"); raw(&IL::pm_sri, "pm_sri");
   raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
   raw(&IL::sp_mw, "sp_mw"); der(&IL::sp_thermo);
+  raw(&IL::rate_aux, "rate_aux"); raw(&IL::plog_ptr, "plog_ptr"); raw(&IL::plog_row, "plog_row");
+  raw(&IL::plog_p, "plog_p"); raw(&IL::plog_lp, "plog_lp"); raw(&IL::plog_dlp, "plog_dlp");
+  raw(&IL::cheb_ptr, "cheb_ptr"); raw(&IL::cheb_nt, "cheb_nt"); raw(&IL::cheb_np, "cheb_np");
+  raw(&IL::cheb_par, "cheb_par"); raw(&IL::cheb_tp, "cheb_tp");
   // every blob section and every derived table must have been placed
   for (auto &w : want) {
     bool found = false;

@@ -354,7 +354,7 @@ template <class CS>
 struct IsKcCol<KcCol<CS>> { static constexpr bool value = true; };
 
 struct State {
-  double T, invT, logT;
+  double T, invT, logT, P;
   const double *tab;
 };
 
@@ -370,11 +370,13 @@ __device__ __forceinline__ double rate(const Tab &t, int row, const State &s,
       return c[0];
     case RATE_NEGEXP:
       return c[0] * exp_t(fma(c[2], s.invT, c[1] * s.logT), s.tab);
-    default: {
+    case RATE_POW: {
       double k = c[0];
       for (int j = 0; j < t.rate_npow[row]; ++j) k *= s.T;
       return k;
     }
+    default:  // PLOG, Chebyshev
+      return pdep_kf(t, row, s.T, s.logT, s.P);
   }
 }
 
@@ -626,6 +628,7 @@ __global__ void __launch_bounds__(256, 1)
     State s;
     s.T = b.T[i];
     const double P = b.P[i];
+    s.P = P;
     s.invT = 1.0 / s.T;
     s.logT = log(s.T);
     s.tab = t.exptab;
@@ -744,6 +747,7 @@ __global__ void __launch_bounds__(DW * 32)
       s.logT = blT[j];
       s.tab = t.exptab;
       const double P = bP[j];
+      s.P = P;
       // concentrations (lanes over species)
       double ys = 0.0, mw = 0.0;
       for (int k = lane; k < N - 1; k += 32) {

@@ -103,16 +103,23 @@ __device__ double kc_exponent(const Tab &t, int j, double T, double logT) {
 }
 
 // fwd (and rev when reversible) of reaction r (rate_subs.py:433-693).
+// PLOG / Chebyshev rows print kf first and use it like a reversible
+// reaction's kf (rate_subs.py:437-448, 503-505).
 template <class CS>
-__device__ void rxn_rates(const Tab &t, int r, double T, double logT,
+__device__ void rxn_rates(const Tab &t, int r, double T, double logT, double pres,
                           const CS &C, double &fwd, double &rev) {
   bool have;
   const double p = conc_product(t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
                                 t.rx_ptr[r + 1], C, have);
   const int j = t.rev_idx[r];
-  if (j >= 0) {
-    const double kf = rate_const(t, r, T, logT);
+  const bool pdep = t.rate_kind[r] >= RATE_PLOG;
+  if (j >= 0 || pdep) {
+    const double kf = pdep ? pdep_kf(t, r, T, logT, pres) : rate_const(t, r, T, logT);
     fwd = have ? p * kf : kf;
+    if (j < 0) {
+      rev = 0.0;
+      return;
+    }
     double Kc = kc_exponent(t, j, T, logT);
     Kc = t.kc_pref[j] * exp(Kc);
     bool hq;
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(128)
     const double mix = P / (8.31446210e+03 * T);
     for (int r = 0; r < t.R; ++r) {
       double fwd, rev;
-      rxn_rates(t, r, T, logT, C, fwd, rev);
+      rxn_rates(t, r, T, logT, P, C, fwd, rev);
       const int j = t.rev_idx[r];
       const int p = t.pm_idx[r];
       double pm = 0.0;
@@ -298,12 +305,12 @@ __global__ void k_rxn_rates(const unsigned char *__restrict__ img, ImgLayout L,
   const Tab t = make_tab(img, L);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double T = b.T[i];
+    const double T = b.T[i], P = b.P[i];
     Col C{b.conc + i, b.ld};
     const double logT = log(T);
     for (int r = 0; r < t.R; ++r) {
       double fwd, rev;
-      rxn_rates(t, r, T, logT, C, fwd, rev);
+      rxn_rates(t, r, T, logT, P, C, fwd, rev);
       b.fwd[(int64_t)r * b.ld + i] = fwd;
       const int j = t.rev_idx[r];
       if (j >= 0 && b.rev) b.rev[(int64_t)j * b.ld + i] = rev;

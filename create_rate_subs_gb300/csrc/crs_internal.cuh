@@ -13,7 +13,9 @@
 
 namespace crs {
 
-enum { RATE_CONST = 0, RATE_EXP = 1, RATE_NEGEXP = 2, RATE_POW = 3 };
+enum { RATE_CONST = 0, RATE_EXP = 1, RATE_NEGEXP = 2, RATE_POW = 3, RATE_PLOG = 4,
+       RATE_CHEB = 5 };
+constexpr int CHEB_MAX = 16;  // most Chebyshev temperature terms (checked at load)
 enum { PM_THD = 0, PM_FALL_LOW = 1, PM_FALL_HIGH = 2 };
 enum { FORM_LINDEMANN = 0, FORM_TROE = 1, FORM_SRI = 2 };
 
@@ -58,6 +60,11 @@ struct ImgLayout {
   // f64 sections
   int inv_mw, rate_par, rx_nu, px_nu, kc_tmid, kc_lo, kc_hi, kc_pref,
       pm_eff_val, pm_troe, pm_sri, nu_val, sp_tmid, sp_lo, sp_hi, kc_dnu, sp_mw;
+  // PLOG and Chebyshev rate forms: per rate row an index into their tables
+  // (rate_aux), PLOG points (printed pressure, ln P, ln-P spacing, rate row)
+  // and Chebyshev coefficient blocks with their reduced-T/P constants
+  int rate_aux, plog_ptr, plog_row, plog_p, plog_lp, plog_dlp, cheb_ptr, cheb_nt, cheb_np,
+      cheb_par, cheb_tp;
   // i32 sections
   int rate_kind, rate_npow, rx_ptr, rx_sp, rx_nint, px_ptr, px_sp, px_nint,
       rev_idx, kc_ptr, pm_idx, pm_kind, pm_form, pm_sp, pm_eff_ptr,
@@ -76,6 +83,8 @@ struct Tab {
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
       *sp_hi, *kc_dnu, *sp_mw;
+  const int32_t *rate_aux, *plog_ptr, *plog_row, *cheb_ptr, *cheb_nt, *cheb_np;
+  const double *plog_p, *plog_lp, *plog_dlp, *cheb_par, *cheb_tp;
   const int32_t *rate_kind, *rate_npow, *rx_ptr, *rx_sp, *rx_nint, *px_ptr,
       *px_sp, *px_nint, *rev_idx, *kc_ptr, *pm_idx, *pm_kind, *pm_form,
       *pm_sp, *pm_eff_ptr, *pm_eff_sp, *pm_k0, *pm_kinf, *pm_troe_t2,
@@ -110,6 +119,9 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
   CRS_F(kc_lo); CRS_F(kc_hi); CRS_F(kc_pref); CRS_F(pm_eff_val);
   CRS_F(pm_troe); CRS_F(pm_sri); CRS_F(nu_val); CRS_F(sp_tmid); CRS_F(sp_lo);
   CRS_F(sp_hi); CRS_F(kc_dnu); CRS_F(sp_mw);
+  CRS_I(rate_aux); CRS_I(plog_ptr); CRS_I(plog_row); CRS_I(cheb_ptr); CRS_I(cheb_nt);
+  CRS_I(cheb_np); CRS_F(plog_p); CRS_F(plog_lp); CRS_F(plog_dlp); CRS_F(cheb_par);
+  CRS_F(cheb_tp);
   CRS_I(rate_kind); CRS_I(rate_npow); CRS_I(rx_ptr); CRS_I(rx_sp);
   CRS_I(rx_nint); CRS_I(px_ptr); CRS_I(px_sp); CRS_I(px_nint); CRS_I(rev_idx);
   CRS_I(kc_ptr); CRS_I(pm_idx); CRS_I(pm_kind); CRS_I(pm_form); CRS_I(pm_sp);
@@ -261,6 +273,81 @@ cudaError_t launch_conc_rho(const unsigned char *img, const ImgLayout &L, int64_
 cudaError_t launch_dydt_finish(const unsigned char *img, const ImgLayout &L, int conv,
                                int64_t n, const double *y, int64_t ld, const double *p_or_rho,
                                const double *W, double *dy, int sm_count, cudaStream_t s);
+
+#ifdef __CUDACC__
+// rxn_rate_const in the emitted form (rate_subs.py:60-135), CUDA exp.
+__device__ inline double ref_rate_const(const Tab &t, int row, double T, double logT) {
+  const double *p = t.rate_par + 4 * row;  // A, logA, b, Ta
+  switch (t.rate_kind[row]) {
+    case RATE_CONST:
+      return p[0];
+    case RATE_EXP:
+      return exp(p[1] + p[2] * logT - (p[3] / T));
+    case RATE_NEGEXP:
+      return p[0] * exp(p[2] * logT - (p[3] / T));
+    default: {
+      double k = p[0];
+      for (int j = 0; j < t.rate_npow[row]; ++j) k = k * T;
+      return k;
+    }
+  }
+}
+
+// Forward rate constant of a PLOG row (rate_subs.py:444-485: branch
+// thresholds as printed with %.4e, log-linear interpolation in ln P between
+// the bracketing points) or a Chebyshev row (rate_subs.py:136-223: reduced
+// temperature and pressure, the pressure dot products by the Chebyshev
+// recursion, then the temperature sum, 10^kf), in the emitted order.
+__device__ inline double pdep_kf(const Tab &t, int row, double T, double logT, double pres) {
+  const int a = t.rate_aux[row];
+  if (t.rate_kind[row] == RATE_PLOG) {
+    const int e0 = t.plog_ptr[a], e1 = t.plog_ptr[a + 1];
+    if (pres <= t.plog_p[e0]) return ref_rate_const(t, t.plog_row[e0], T, logT);
+    for (int e = e0; e < e1 - 1; ++e)
+      if ((pres > t.plog_p[e]) && (pres <= t.plog_p[e + 1])) {
+        const double k1 = log(ref_rate_const(t, t.plog_row[e], T, logT));
+        const double k2 = log(ref_rate_const(t, t.plog_row[e + 1], T, logT));
+        return exp(k1 + (k2 - k1) * (log(pres) - t.plog_lp[e]) / t.plog_dlp[e]);
+      }
+    if (pres > t.plog_p[e1 - 1]) return ref_rate_const(t, t.plog_row[e1 - 1], T, logT);
+    return __longlong_as_double(0x7ff8000000000000ll);  // no branch (NaN pressure)
+  }
+  const double *tp = t.cheb_tp + 4 * a;
+  const int nt = t.cheb_nt[a], np = t.cheb_np[a];
+  const double *c = t.cheb_par + t.cheb_ptr[a];  // [nt][np]
+  const double Tred = ((2.0 / T) - tp[0]) / tp[1];
+  const double Pred = (2.0 * log10(pres) - tp[2]) / tp[3];
+  double dp[CHEB_MAX];
+  for (int i = 0; i < nt; ++i) dp[i] = c[i * np] + Pred * c[i * np + 1];
+  double ct0 = 1.0, ct1 = Pred;
+  bool upd = true;
+  for (int j = 2; j < np; ++j) {
+    if (upd) {
+      ct0 = 2.0 * Pred * ct1 - ct0;
+      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct0;
+    } else {
+      ct1 = 2.0 * Pred * ct0 - ct1;
+      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct1;
+    }
+    upd = !upd;
+  }
+  ct0 = 1.0;
+  ct1 = Tred;
+  double kf = dp[0] + Tred * dp[1];
+  upd = true;
+  for (int i = 2; i < nt; ++i) {
+    if (upd) {
+      ct0 = 2.0 * Tred * ct1 - ct0;
+      kf += dp[i] * ct0;
+    } else {
+      ct1 = 2.0 * Tred * ct0 - ct1;
+      kf += dp[i] * ct1;
+    }
+    upd = !upd;
+  }
+  return pow(10.0, kf);
+}
+#endif
 
 #ifdef __CUDACC__
 // Exponent of the equilibrium constant of reversible reaction j (with ln

@@ -207,7 +207,7 @@ struct DArr {
 };
 
 struct State {
-  double T, invT, logT;
+  double T, invT, logT, P;
   float Tf;
   ff Tff, lTff, iTff;
 };
@@ -470,7 +470,15 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   // the FP64 Kc exponent first, to overlap with the FP32 forward rate
   const double g = j >= 0 ? kc(t, r, j) : 0.0;
   float sgn;
-  const ff xf = rate_exponent(t, r, s, sgn);
+  ff xf;
+  if (t.rate_kind[r] >= RATE_PLOG) {
+    // PLOG / Chebyshev: kf in FP64 in the emitted form, then its log
+    const double kf = pdep_kf(t, r, s.T, s.logT, s.P);
+    sgn = kf < 0.0 ? -1.0f : 1.0f;
+    xf = ff_from_double(log(fabs(kf)));
+  } else {
+    xf = rate_exponent(t, r, s, sgn);
+  }
   int Ef;
   const float pf = ff_exp(xf, Ef);
   const float mf = sgn * product(pf, t.rx_sp, t.rx_nint, t.rx_nu, t.rx_ptr[r],
@@ -540,6 +548,7 @@ __global__ void __launch_bounds__(352, 1)
     State s;
     s.T = b.T[i];
     const double P = b.P[i];
+    s.P = P;
     s.invT = 1.0 / s.T;
     s.logT = log(s.T);
     s.Tf = (float)s.T;
@@ -649,6 +658,7 @@ __global__ void __launch_bounds__(DW * 32)
       s.lTff = ff_from_double(s.logT);
       s.iTff = ff_from_double(s.invT);
       const double P = bP[j];
+      s.P = P;
       double ys = 0.0, mw = 0.0;
       for (int k = lane; k < N - 1; k += 32) {
         const double y = b.Y[(int64_t)k * b.ld + i];

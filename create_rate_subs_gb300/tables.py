@@ -11,6 +11,11 @@ Where each table comes from in the reference:
   CONST (``A``), EXP (``exp(logA + b*logT - Ta/T)``), NEGEXP
   (``A*exp(b*logT - Ta/T)``, A<0), POW (``A*T*...*T``, A<0 with integral b
   and no E, or an ``int`` b).  ``logA`` is ``math.log(A)``, printed %.16e.
+* PLOG (rate_subs.py:444-485): per pressure point a rate row; the branch
+  thresholds are the pressures as printed with %.4e, the interpolation
+  uses ``math.log(P)`` and the log spacing (printed %.16e, exact).
+* Chebyshev (rate_subs.py:136-223): the coefficients and the reduced
+  temperature / pressure constants as printed with %.8e.
 * Kc groups: rate_subs.py:513-662 (per reaction, species coefficients summed
   on the host and grouped by T_common; prefactor ``(PA/RU)**sum_nu``).
 * pressure modification: rate_subs.py:881-1064 (efficiencies as ``eff-1``,
@@ -31,12 +36,14 @@ import numpy as np
 from . import chem
 from .utils import get_nu, is_integer
 
-__all__ = ["RATE_CONST", "RATE_EXP", "RATE_NEGEXP", "RATE_POW",
+__all__ = ["RATE_CONST", "RATE_EXP", "RATE_NEGEXP", "RATE_POW", "RATE_PLOG", "RATE_CHEB",
            "PM_THD", "PM_FALL_LOW", "PM_FALL_HIGH",
            "FORM_LINDEMANN", "FORM_TROE", "FORM_SRI",
            "build_tables", "pack", "unpack", "BLOB_MAGIC"]
 
 RATE_CONST, RATE_EXP, RATE_NEGEXP, RATE_POW = 0, 1, 2, 3
+RATE_PLOG, RATE_CHEB = 4, 5
+CHEB_MAX = 16  # most Chebyshev temperature terms the kernels accept
 PM_THD, PM_FALL_LOW, PM_FALL_HIGH = 0, 1, 2
 FORM_LINDEMANN, FORM_TROE, FORM_SRI = 0, 1, 2
 
@@ -161,12 +168,49 @@ def build_tables(specs, reacs):
               sri_de=[])
     n_rev = n_pm = 0
 
+    rate_aux = []
+    plog = dict(ptr=[0], p=[], lp=[], dlp=[], row=[])
+    cheb = dict(ptr=[0], nt=[], np=[], par=[], tp=[])
+    plog_pending = []
     for r, rxn in enumerate(reacs):
-        if rxn.cheb or rxn.plog:
-            raise NotImplementedError(
-                "reaction %d: Chebyshev/PLOG rate forms are not supported by "
-                "the table-driven kernels yet" % r)
-        rates.append(rate_record(rxn.A, rxn.b, rxn.E))
+        if rxn.plog:
+            rates.append((RATE_PLOG, 0, 0.0, 0.0, 0.0, 0.0))
+            rate_aux.append(len(plog["ptr"]) - 1)
+            pts = list(rxn.plog_par)
+            for i, (P, A, b, E) in enumerate(pts):
+                plog["p"].append(float("{:.4e}".format(P)))
+                plog["lp"].append(math.log(P))
+                plog["dlp"].append(math.log(pts[i + 1][0]) - math.log(P)
+                                   if i + 1 < len(pts) else 1.0)
+                plog_pending.append((A, b, E))
+            plog["ptr"].append(len(plog["p"]))
+        elif rxn.cheb:
+            nt, npr = int(rxn.cheb_n_temp), int(rxn.cheb_n_pres)
+            if nt < 2 or npr < 2 or nt > CHEB_MAX:
+                raise NotImplementedError(
+                    "reaction %d: Chebyshev needs 2..%d temperature and >= 2 "
+                    "pressure terms (the emitted code indexes terms 0 and 1)"
+                    % (r, CHEB_MAX))
+            rates.append((RATE_CHEB, 0, 0.0, 0.0, 0.0, 0.0))
+            rate_aux.append(len(cheb["nt"]))
+            par = np.asarray(rxn.cheb_par, dtype=np.float64).reshape(nt, npr)
+            cheb["par"].extend(_fmt8(float(x)) for x in par.ravel())
+            cheb["ptr"].append(len(cheb["par"]))
+            cheb["nt"].append(nt)
+            cheb["np"].append(npr)
+            t0, t1 = rxn.cheb_tlim
+            p0, p1 = rxn.cheb_plim
+            cheb["tp"].append([_fmt8(1.0 / t0 + 1.0 / t1), _fmt8(1.0 / t1 - 1.0 / t0),
+                               _fmt8(math.log10(p0) + math.log10(p1)),
+                               _fmt8(math.log10(p1) - math.log10(p0))])
+        else:
+            rates.append(rate_record(rxn.A, rxn.b, rxn.E))
+            rate_aux.append(-1)
+    # the PLOG pressure points' own Arrhenius rows follow the reactions' rows
+    for (A, b, E) in plog_pending:
+        plog["row"].append(len(rates))
+        rates.append(rate_record(A, b, E))
+        rate_aux.append(-1)
     for r, rxn in enumerate(reacs):
         for (names, nus, dst) in ((rxn.reac, rxn.reac_nu, rx),
                                   (rxn.prod, rxn.prod_nu, px)):
@@ -208,11 +252,13 @@ def build_tables(specs, reacs):
                 if rxn.low:
                     pm["kind"].append(PM_FALL_LOW)
                     rates.append(rate_record(*rxn.low))
+                    rate_aux.append(-1)
                     pm["k0"].append(len(rates) - 1)
                     pm["kinf"].append(r)
                 elif rxn.high:
                     pm["kind"].append(PM_FALL_HIGH)
                     rates.append(rate_record(*rxn.high))
+                    rate_aux.append(-1)
                     pm["k0"].append(r)
                     pm["kinf"].append(len(rates) - 1)
                 else:
@@ -278,6 +324,12 @@ def build_tables(specs, reacs):
     t["rate_kind"] = i32([x[0] for x in rates])
     t["rate_npow"] = i32([x[1] for x in rates])
     t["rate_par"] = f64([x[2:] for x in rates]).reshape(len(rates), 4)
+    t["rate_aux"] = i32(rate_aux)
+    t["plog_ptr"], t["plog_row"] = i32(plog["ptr"]), i32(plog["row"])
+    t["plog_p"], t["plog_lp"], t["plog_dlp"] = f64(plog["p"]), f64(plog["lp"]), f64(plog["dlp"])
+    t["cheb_ptr"], t["cheb_nt"], t["cheb_np"] = i32(cheb["ptr"]), i32(cheb["nt"]), i32(cheb["np"])
+    t["cheb_par"] = f64(cheb["par"])
+    t["cheb_tp"] = f64(cheb["tp"]).reshape(len(cheb["nt"]), 4)
     t["rx_ptr"], t["rx_sp"], t["rx_nu"], t["rx_nint"] = i32(rx[3]), i32(rx[0]), f64(rx[1]), i32(rx[2])
     t["px_ptr"], t["px_sp"], t["px_nu"], t["px_nint"] = i32(px[3]), i32(px[0]), f64(px[1]), i32(px[2])
     t["rev_idx"] = i32(rev_idx)
@@ -356,7 +408,7 @@ def unpack(blob):
         out[name.rstrip(b"\0").decode()] = np.frombuffer(
             blob, dtype=dt, count=count, offset=off).copy()
     for name, w in (("sp_lo", 7), ("sp_hi", 7), ("kc_lo", 7), ("kc_hi", 7),
-                    ("rate_par", 4), ("pm_troe", 5), ("pm_sri", 5)):
+                    ("rate_par", 4), ("pm_troe", 5), ("pm_sri", 5), ("cheb_tp", 4)):
         if name in out:
             out[name] = out[name].reshape(-1, w)
     return out

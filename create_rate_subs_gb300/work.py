@@ -9,7 +9,7 @@ counts 2 flops, a divide 1, a call to exp/log/log10/pow one transcendental.
 """
 
 from .tables import (FORM_SRI, FORM_TROE, PM_THD, RATE_CONST, RATE_EXP,
-                     RATE_NEGEXP)
+                     RATE_NEGEXP, RATE_POW)
 
 __all__ = ["state_bytes", "work"]
 
@@ -26,7 +26,12 @@ def _rate(kind, npow):
         return 4, 1          # b*logT, +, Ta/T, -, exp
     if kind == RATE_NEGEXP:
         return 4, 1          # b*logT, Ta/T, -, exp, A*
-    return npow, 0
+    if kind == RATE_POW:
+        return npow, 0
+    # PLOG (two rate rows, two logs, one exp and the interpolation) and
+    # Chebyshev (reduced T, P and the dot products, one pow) are counted
+    # roughly; no benchmark mechanism uses them
+    return 12, 5
 
 
 def work(tables):

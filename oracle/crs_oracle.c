@@ -31,7 +31,9 @@
 #include <omp.h>
 #endif
 
-enum { RATE_CONST = 0, RATE_EXP = 1, RATE_NEGEXP = 2, RATE_POW = 3 };
+enum { RATE_CONST = 0, RATE_EXP = 1, RATE_NEGEXP = 2, RATE_POW = 3, RATE_PLOG = 4,
+       RATE_CHEB = 5 };
+#define CHEB_MAX 16
 enum { PM_THD = 0, PM_FALL_LOW = 1, PM_FALL_HIGH = 2 };
 enum { FORM_LINDEMANN = 0, FORM_TROE = 1, FORM_SRI = 2 };
 
@@ -52,6 +54,8 @@ typedef struct {
   const int32_t *nu_ptr, *nu_sp;
   const double *nu_val;
   const double *sp_mw, *sp_tmid, *sp_lo, *sp_hi;
+  const int32_t *rate_aux, *plog_ptr, *plog_row, *cheb_ptr, *cheb_nt, *cheb_np;
+  const double *plog_p, *plog_lp, *plog_dlp, *cheb_par, *cheb_tp;
   unsigned char *blob; /* owned copy */
 } omech;
 
@@ -111,11 +115,16 @@ int oracle_load(const void *blob, size_t n, omech **out) {
   F64(pm_eff_val, "pm_eff_val"); F64(pm_troe, "pm_troe"); F64(pm_sri, "pm_sri");
   I32(nu_ptr, "nu_ptr"); I32(nu_sp, "nu_sp"); F64(nu_val, "nu_val");
   F64(sp_mw, "sp_mw"); F64(sp_tmid, "sp_tmid"); F64(sp_lo, "sp_lo"); F64(sp_hi, "sp_hi");
+  I32(rate_aux, "rate_aux"); I32(plog_ptr, "plog_ptr"); I32(plog_row, "plog_row");
+  I32(cheb_ptr, "cheb_ptr"); I32(cheb_nt, "cheb_nt"); I32(cheb_np, "cheb_np");
+  F64(plog_p, "plog_p"); F64(plog_lp, "plog_lp"); F64(plog_dlp, "plog_dlp");
+  F64(cheb_par, "cheb_par"); F64(cheb_tp, "cheb_tp");
 #undef F64
 #undef I32
   if (!m->inv_mw || !m->rate_kind || !m->rx_ptr || !m->px_ptr || !m->rev_idx ||
       !m->pm_idx || !m->nu_ptr || !m->kc_ptr || !m->pm_eff_ptr || !m->sp_mw ||
-      !m->sp_tmid || !m->sp_lo || !m->sp_hi) {
+      !m->sp_tmid || !m->sp_lo || !m->sp_hi || !m->rate_aux || !m->plog_ptr ||
+      !m->cheb_ptr) {
     oracle_free(m);
     return 3;
   }
@@ -142,6 +151,61 @@ static double rate_const(const omech *m, int row, double T, double logT) {
       for (int i = 0; i < m->rate_npow[row]; ++i) k = k * T;
       return k;
   }
+}
+
+/* PLOG (rate_subs.py:444-485) and Chebyshev (rate_subs.py:136-223) forward
+ * rate constants, in the emitted order: PLOG branches on the pressures as
+ * printed with %.4e and interpolates log-linearly in ln P; Chebyshev forms
+ * the reduced T and P, the pressure dot products by the Chebyshev
+ * recursion, the temperature sum and 10^kf. */
+static double pdep_kf(const omech *m, int row, double T, double logT, double pres) {
+  const int a = m->rate_aux[row];
+  if (m->rate_kind[row] == RATE_PLOG) {
+    const int e0 = m->plog_ptr[a], e1 = m->plog_ptr[a + 1];
+    if (pres <= m->plog_p[e0]) return rate_const(m, m->plog_row[e0], T, logT);
+    for (int e = e0; e < e1 - 1; ++e)
+      if ((pres > m->plog_p[e]) && (pres <= m->plog_p[e + 1])) {
+        double kf = log(rate_const(m, m->plog_row[e], T, logT));
+        double kf2 = log(rate_const(m, m->plog_row[e + 1], T, logT));
+        return exp(kf + (kf2 - kf) * (log(pres) - m->plog_lp[e]) / m->plog_dlp[e]);
+      }
+    if (pres > m->plog_p[e1 - 1]) return rate_const(m, m->plog_row[e1 - 1], T, logT);
+    return NAN;
+  }
+  const double *tp = m->cheb_tp + 4 * a;
+  const int nt = m->cheb_nt[a], np = m->cheb_np[a];
+  const double *c = m->cheb_par + m->cheb_ptr[a];
+  double Tred = ((2.0 / T) - tp[0]) / tp[1];
+  double Pred = (2.0 * log10(pres) - tp[2]) / tp[3];
+  double dp[CHEB_MAX];
+  for (int i = 0; i < nt; ++i) dp[i] = c[i * np] + Pred * c[i * np + 1];
+  double ct0 = 1, ct1 = Pred;
+  int upd = 1;
+  for (int j = 2; j < np; ++j) {
+    if (upd) {
+      ct0 = 2 * Pred * ct1 - ct0;
+      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct0;
+    } else {
+      ct1 = 2 * Pred * ct0 - ct1;
+      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct1;
+    }
+    upd = !upd;
+  }
+  ct0 = 1;
+  ct1 = Tred;
+  double kf = dp[0] + Tred * dp[1];
+  upd = 1;
+  for (int i = 2; i < nt; ++i) {
+    if (upd) {
+      ct0 = 2 * Tred * ct1 - ct0;
+      kf += dp[i] * ct0;
+    } else {
+      ct1 = 2 * Tred * ct0 - ct1;
+      kf += dp[i] * ct1;
+    }
+    upd = !upd;
+  }
+  return pow(10.0, kf);
 }
 
 /* Product of concentrations C[k]^nu over one side, left to right, integral
@@ -184,15 +248,19 @@ static double kc_exponent(const omech *m, int j, double T, double logT) {
 
 void oracle_eval_rxn_rates(const omech *m, double T, double pres,
                            const double *C, double *fwd, double *rev) {
-  (void)pres;
   double logT = log(T);
   for (int r = 0; r < m->R; ++r) {
     int have;
     double p = conc_product(m->rx_sp, m->rx_nint, m->rx_nu, m->rx_ptr[r],
                             m->rx_ptr[r + 1], C, &have);
     int j = m->rev_idx[r];
-    if (j >= 0) {
-      double kf = rate_const(m, r, T, logT);
+    const int pdep = m->rate_kind[r] >= RATE_PLOG;
+    if (pdep && j < 0) {
+      /* PLOG / Chebyshev print kf first, then C... * kf (:437-448, 503-505) */
+      double kf = pdep_kf(m, r, T, logT, pres);
+      fwd[r] = have ? p * kf : kf;
+    } else if (j >= 0) {
+      double kf = pdep ? pdep_kf(m, r, T, logT, pres) : rate_const(m, r, T, logT);
       fwd[r] = have ? p * kf : kf;
       double Kc = kc_exponent(m, j, T, logT);
       Kc = m->kc_pref[j] * exp(Kc);

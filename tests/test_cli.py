@@ -30,7 +30,7 @@ def test_gb300_target_writes_tables_and_headers(tmp_path):
         assert (out / f).exists(), f
     blob = (out / "mech.crs").read_bytes()
     t = tables.unpack(blob)
-    assert [int(x) for x in t["dims"][:4]] == [10, 22, 16, 8]
+    assert [int(x) for x in t["dims"][:4]] == [10, 26, 18, 8]
     info = (ctypes.c_int64 * 6)()
     assert _lib.load().crs_mech_inspect(blob, len(blob), info) == 0
     names = re.findall(r"^ \* \d+ (\S+)$", (out / "header.h").read_text(), re.M)
