@@ -7,6 +7,7 @@
 #include <cstring>
 #include <fstream>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -47,6 +48,10 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
                        const ImgLayout &L, std::vector<Derived> &extra);
 }  // namespace crs
 
+// Dynamic-scheduling slots per mechanism handle: the most launches of the
+// one-state-per-thread kernels that may run at the same time on one handle.
+constexpr unsigned SCHED_SLOTS = 256;
+
 struct crs_mech {
   int device = 0;
   int sm_count = 0;
@@ -54,6 +59,11 @@ struct crs_mech {
   crs::ImgLayout L{};
   unsigned char *d_img = nullptr;  // device table image
   int32_t *d_status = nullptr;     // [0] flags, [1] non-finite count
+  // dynamic-scheduling counter pairs of the one-state-per-thread kernels;
+  // each launch draws the next slot, so launches in flight at the same time
+  // (several streams) use different counters
+  unsigned long long *d_sched = nullptr;
+  mutable std::atomic<unsigned> sched_next{0};
   std::vector<unsigned char> h_img;
   // tensor-core contraction (CRS_MODE_GEMM): nu as a bf16 matrix
   // [N_pad][2*Kh] (each row nu_k, then nu_k again for the lo half), and a
@@ -286,6 +296,12 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
     return fail(CRS_ERR_BLOB, "could not derive fast tables");
   L.kc_single = 1;
   for (int j = 0; j < L.NREV; ++j) L.kc_single &= (t.kc_ptr[j + 1] - t.kc_ptr[j]) <= 1;
+  L.nu_hi_exact = 1;
+  for (int e = 0; e < t.nu_ptr[L.R]; ++e) {
+    uint64_t u;
+    memcpy(&u, &t.nu_val[e], 8);
+    L.nu_hi_exact &= (u & 0xffffffffull) == 0;
+  }
   using M = int crs::ImgLayout::*;
   std::vector<std::pair<M, std::vector<unsigned char>>> secs;
   auto raw = [&](M f, const char *name) {
@@ -315,14 +331,15 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   raw(&IL::rx_sp, "rx_sp"); raw(&IL::rx_nint, "rx_nint");
   raw(&IL::px_ptr, "px_ptr"); raw(&IL::px_sp, "px_sp");
   raw(&IL::px_nint, "px_nint");
+  raw(&IL::nu_sp, "nu_sp"); raw(&IL::nu_val, "nu_val");
   const size_t iS1 = secs.size();
   // [S1] shared by all fast kernels
   raw(&IL::inv_mw, "sp_inv_mw");
   raw(&IL::rev_idx, "rev_idx"); raw(&IL::pm_idx, "pm_idx");
-  raw(&IL::nu_ptr, "nu_ptr"); raw(&IL::nu_sp, "nu_sp"); raw(&IL::nu_val, "nu_val");
+  raw(&IL::nu_ptr, "nu_ptr");
   const size_t iM = secs.size();
-  // [M] mixed only
-  der(&IL::rate_ff); der(&IL::inv_mw_f);
+  // [M] mixed only (the net-nu lists in their compact form)
+  der(&IL::rate_ff); der(&IL::inv_mw_f); der(&IL::nu_sp16); der(&IL::nu_hi);
   const size_t iK = secs.size();
   // [K] per-reaction Kc polynomials (mixed, one state per thread) and the
   // ln Kc prefactors (read through L1 by the Gibbs-column layouts)
@@ -412,6 +429,7 @@ crs::Batch make_batch(const crs_mech *m, int64_t n, int64_t ld) {
   b.n = n;
   b.ld = ld;
   b.status = m->d_status;
+  b.sched = m->d_sched ? m->d_sched + 2 * (m->sched_next.fetch_add(1) % SCHED_SLOTS) : nullptr;
   return b;
 }
 
@@ -563,13 +581,17 @@ int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
     e = cudaMemcpy(m->d_img, m->h_img.data(), m->h_img.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&m->d_status, 4 * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, 4 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_sched, 2 * SCHED_SLOTS * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(m->d_sched, 0, 2 * SCHED_SLOTS * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     int r = cuda_fail(e, "crs_mech_load");
     crs_mech_free(m);
     return r;
   }
-  // reserve the static __shared__ mbarrier and a little slack
-  m->smem_optin -= 64;
+  // dynamic shared memory of the launchers: the opt-in limit less the
+  // kernels' static __shared__ part (the staging mbarrier, which the
+  // 128-byte alignment of the dynamic part pads to 128 bytes) and slack
+  m->smem_optin -= 256;
   *out = m;
   return CRS_OK;
 }
@@ -606,6 +628,7 @@ int crs_mech_free(crs_mech *m) {
   if (!m) return CRS_OK;
   if (m->d_img) cudaFree(m->d_img);
   if (m->d_status) cudaFree(m->d_status);
+  if (m->d_sched) cudaFree(m->d_sched);
   if (m->d_nuB) cudaFree(m->d_nuB);
   if (m->d_ws) cudaFree(m->d_ws);
   if (m->d_escale) cudaFree(m->d_escale);

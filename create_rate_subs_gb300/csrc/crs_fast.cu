@@ -213,14 +213,35 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
       }
     }
   }
-  std::vector<int32_t> perm, seg(NSHAPE + 1);
+  // seg[NSHAPE] .. seg[NSHAPE + 1]: the other reactions of exponential
+  // form; seg[NSHAPE + 1] .. R: PLOG and Chebyshev reactions, last, so that
+  // the hot general loop of the one-state-per-thread kernels has no code
+  // for them
+  std::vector<int32_t> perm, seg(NSHAPE + 2);
   for (int sh = 0; sh <= NSHAPE; ++sh) {
     seg[sh] = (int32_t)perm.size();
     for (int r = 0; r < L.R; ++r)
-      if (shape[r] == sh) perm.push_back(r);
+      if (shape[r] == sh && (sh < NSHAPE || t.rate_kind[r] < RATE_PLOG)) perm.push_back(r);
   }
+  seg[NSHAPE + 1] = (int32_t)perm.size();
+  for (int r = 0; r < L.R; ++r)
+    if (shape[r] == NSHAPE && t.rate_kind[r] >= RATE_PLOG) perm.push_back(r);
   if (perm.empty()) perm.push_back(0);
   put(extra, &ImgLayout::perm, perm);
+  // net-nu entries in compact form for the mixed one-state-per-thread kernel
+  {
+    const int nnz = t.nu_ptr[L.R];
+    std::vector<int16_t> sp16(nnz > 0 ? nnz : 1, 0);
+    std::vector<int32_t> hi(nnz > 0 ? nnz : 1, 0);
+    for (int e = 0; e < nnz; ++e) {
+      uint64_t u;
+      memcpy(&u, &t.nu_val[e], 8);
+      sp16[e] = (int16_t)t.nu_sp[e];
+      hi[e] = (int32_t)(u >> 32);
+    }
+    put(extra, &ImgLayout::nu_sp16, sp16);
+    put(extra, &ImgLayout::nu_hi, hi);
+  }
   // warp-per-state kernels: reactions ordered so that 32 consecutive ones
   // mostly take the same code path (rate form, pressure modification,
   // broadening, reversibility, factor counts)
@@ -453,11 +474,17 @@ __device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
   for (int u = 0; u < 4; ++u) {
     if (u >= cnt) break;
     const int e0 = t.nu_ptr[rr[u]];
+    // the species of one reaction are distinct: all its loads go before its
+    // stores, so that they overlap instead of waiting on each other
+    int k[NNU];
+    double w[NNU];
 #pragma unroll
     for (int q = 0; q < NNU; ++q) {
-      const int k = t.nu_sp[e0 + q];
-      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);
+      k[q] = t.nu_sp[e0 + q];
+      w[q] = W[k[q]];
     }
+#pragma unroll
+    for (int q = 0; q < NNU; ++q) W[k[q]] = fma(t.nu_val[e0 + q], net[u], w[q]);
   }
 }
 
@@ -613,9 +640,14 @@ __global__ void __launch_bounds__(256, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
+  const unsigned amask = __activemask();
+  const int lane = threadIdx.x & 31;
   Tab t;
   int nb;
-  if (!stage_ranges(smem, img, L, 0, &bar, b.status, t, nb)) return;
+  if (!stage_ranges(smem, img, L, 0, &bar, b.status, t, nb)) {
+    sched_done(b.sched, amask, lane);
+    return;
+  }
   const int N = t.N;
   double *base = reinterpret_cast<double *>(smem + nb);
   const int64_t st = blockDim.x;
@@ -623,8 +655,16 @@ __global__ void __launch_bounds__(256, 1)
   const Col W{base + (int64_t)N * st + threadIdx.x, st};
   const Col S{base + (int64_t)2 * N * st + threadIdx.x, st};  // KCM 0 only
   int bad = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - (int64_t)gridDim.x * blockDim.x;
+  for (;;) {
+    if (b.sched) {
+      i = sched_next(b.sched, b.n, amask, lane);
+      if (i < 0) break;
+      if (i >= b.n) continue;
+    } else {
+      i += (int64_t)gridDim.x * blockDim.x;
+      if (i >= b.n) break;
+    }
     State s;
     s.T = b.T[i];
     const double P = b.P[i];
@@ -685,6 +725,7 @@ __global__ void __launch_bounds__(256, 1)
     }
   }
   if (bad && b.status) atomicAdd(&b.status[1], bad);
+  sched_done(b.sched, amask, lane);
 }
 
 // ---- warp per state -----------------------------------------------------

@@ -47,6 +47,10 @@ struct ImgLayout {
   // exponent polynomial with ln(prefactor) folded into c0; built when every
   // reaction has a single T_common group (kc_single = 1)
   int kc_poly, kc_single;
+  // derived sections (mixed, one state per thread): the net-nu species as
+  // int16 and each nu as the high word of its double (nu_hi_exact = 1 when
+  // every nu's low word is zero, i.e. the pair is exact)
+  int nu_sp16, nu_hi, nu_hi_exact;
   // derived f64 section (thermo utilities): per species 24 doubles
   // [RU/mw, mw, T_common, 0, lo: a0..a5, a1/2, a2/3, a3/4, a4/5, hi: same]
   int sp_thermo;
@@ -80,6 +84,8 @@ struct Tab {
   const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
   const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly, *sp_thermo;
   int kc_single;
+  const int16_t *nu_sp16;
+  const int32_t *nu_hi;
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
       *sp_hi, *kc_dnu, *sp_mw;
@@ -112,6 +118,8 @@ __host__ __device__ inline Tab make_tab2(const unsigned char *near,
   CRS_I(perm); CRS_I(seg);
   t.rfac = reinterpret_cast<const int16_t *>(CRS_P(rfac));
   t.pfac = reinterpret_cast<const int16_t *>(CRS_P(pfac));
+  t.nu_sp16 = reinterpret_cast<const int16_t *>(CRS_P(nu_sp16));
+  CRS_I(nu_hi);
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
   CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
@@ -165,9 +173,50 @@ struct Batch {
   const double *T, *P, *Y;
   double *wdot, *conc, *fwd, *rev, *pm;
   int32_t *status;  // [0] flag bits, [1] non-finite wdot count
+  // dynamic scheduling slot of the one-state-per-thread kernels: [0] states
+  // handed out, [1] warps finished (both zero between launches); null: a
+  // static grid stride
+  unsigned long long *sched;
 };
 
 #ifdef __CUDACC__
+// ---- dynamic state scheduling -------------------------------------------
+// The one-state-per-thread kernels run one CTA per SM whose thread count is
+// set by shared memory, rarely a multiple of 4 warps, so the SM's four
+// sub-partitions hold unequal numbers of warps.  With a static grid stride
+// every warp evaluates the same number of states and the sub-partitions
+// with more warps finish last; handing out states one warp-sized chunk at a
+// time from a global counter lets the faster warps take more.
+
+// Next chunk of states for the calling warp: its first state + lane (past n
+// for some lanes of the last chunk), or -1 for every lane when the batch is
+// exhausted.  amask: the
+// warp's lanes (taken at kernel entry, when the warp is converged).
+__device__ __forceinline__ int64_t sched_next(unsigned long long *sched, int64_t n,
+                                              unsigned amask, int lane) {
+  unsigned long long got = 0;
+  if (lane == 0) got = atomicAdd(sched, (unsigned long long)__popc(amask));
+  got = __shfl_sync(amask, got, 0);
+  return got >= (unsigned long long)n ? -1 : (int64_t)got + lane;
+}
+
+// Called once by every warp of the launch when it is done (also on early
+// exits): the last one puts the slot back to zero for the next launch that
+// draws it.  Counters only; no wait.
+__device__ __forceinline__ void sched_done(unsigned long long *sched, unsigned amask, int lane) {
+  if (!sched) return;
+  __syncwarp(amask);
+  if (lane == 0) {
+    const unsigned long long warps =
+        (unsigned long long)gridDim.x * ((blockDim.x + 31) / 32);
+    __threadfence();
+    if (atomicAdd(sched + 1, 1ULL) == warps - 1) {
+      atomicExch(sched, 0ULL);
+      atomicExch(sched + 1, 0ULL);
+    }
+  }
+}
+
 // ---- shared-memory staging with cp.async.bulk + mbarrier ---------------
 // Every wait is bounded: on expiry the CTA records STATUS_STAGE_TIMEOUT and
 // the caller skips its work.

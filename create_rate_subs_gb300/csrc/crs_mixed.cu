@@ -360,11 +360,18 @@ __device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
   for (int u = 0; u < 4; ++u) {
     if (u >= cnt) break;
     const int e0 = t.nu_ptr[rr[u]];
+    // the species of one reaction are distinct: all its loads go before its
+    // stores, so that they overlap instead of waiting on each other
+    int k[NNU];
+    double w[NNU];
 #pragma unroll
     for (int q = 0; q < NNU; ++q) {
-      const int k = t.nu_sp[e0 + q];
-      W[k] = fma(t.nu_val[e0 + q], net[u], W[k]);  // FP64 accumulation
+      k[q] = t.nu_sp16[e0 + q];
+      w[q] = W[k[q]];
     }
+#pragma unroll
+    for (int q = 0; q < NNU; ++q)
+      W[k[q]] = fma(__hiloint2double(t.nu_hi[e0 + q], 0), net[u], w[q]);  // FP64
   }
 }
 
@@ -461,8 +468,9 @@ struct Shapes<NSHAPE, STAGES, KC> {
                                              int64_t) {}
 };
 
-// Net rate (fwd - rev) * pres_mod of any reaction, as FP64.
-template <class FC, class KC>
+// Net rate (fwd - rev) * pres_mod of any reaction, as FP64.  PD: the
+// reaction may be PLOG or Chebyshev (false: exponential form known).
+template <bool PD = true, class FC, class KC>
 __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
                                           float mix, const FC &C, const KC &kc,
                                           double &fwd, double &rev, float &pm) {
@@ -471,7 +479,7 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   const double g = j >= 0 ? kc(t, r, j) : 0.0;
   float sgn;
   ff xf;
-  if (t.rate_kind[r] >= RATE_PLOG) {
+  if (PD && t.rate_kind[r] >= RATE_PLOG) {
     // PLOG / Chebyshev: kf in FP64 in the emitted form, then its log
     const double kf = pdep_kf(t, r, s.T, s.logT, s.P);
     sgn = kf < 0.0 ? -1.0f : 1.0f;
@@ -503,14 +511,14 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   return net;
 }
 
-template <bool STAGES, class KC>
+template <bool STAGES, bool PD, class KC>
 __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
                                         float mix, const FCol &C,
                                         const KC &S, const DCol &W,
                                         const Batch &b, int64_t i) {
   double fwd, rev;
   float pm;
-  const double net = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
+  const double net = rxn_net<PD>(t, r, s, mix, C, S, fwd, rev, pm);
   if (STAGES) {
     const int j = t.rev_idx[r], p = t.pm_idx[r];
     if (b.fwd) b.fwd[(int64_t)r * b.ld + i] = fwd;
@@ -518,8 +526,8 @@ __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
     if (b.pm && p >= 0) b.pm[(int64_t)p * b.ld + i] = (double)pm;
   }
   for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
-    const int k = t.nu_sp[e];
-    W[k] = fma(t.nu_val[e], net, W[k]);  // FP64 accumulation
+    const int k = t.nu_sp16[e];
+    W[k] = fma(__hiloint2double(t.nu_hi[e], 0), net, W[k]);  // FP64 accumulation
   }
 }
 
@@ -534,17 +542,30 @@ __global__ void __launch_bounds__(352, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
+  const unsigned amask = __activemask();
+  const int lane = threadIdx.x & 31;
   Tab t;
   int nb = 0;
-  if (!stage_ranges(smem, img, L, 2, &bar, b.status, t, nb)) return;
+  if (!stage_ranges(smem, img, L, 2, &bar, b.status, t, nb)) {
+    sched_done(b.sched, amask, lane);
+    return;
+  }
   const int N = t.N;
   const int st = blockDim.x;
   double *dbase = reinterpret_cast<double *>(smem + nb);
   const DCol W{dbase + threadIdx.x, st};
   const FCol C{reinterpret_cast<float *>(dbase + N * st) + threadIdx.x, st};
   int bad = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - (int64_t)gridDim.x * blockDim.x;
+  for (;;) {
+    if (b.sched) {
+      i = sched_next(b.sched, b.n, amask, lane);
+      if (i < 0) break;
+      if (i >= b.n) continue;
+    } else {
+      i += (int64_t)gridDim.x * blockDim.x;
+      if (i >= b.n) break;
+    }
     State s;
     s.T = b.T[i];
     const double P = b.P[i];
@@ -562,12 +583,13 @@ __global__ void __launch_bounds__(352, 1)
       const double y = b.Y[(int64_t)k * b.ld + i];
       ysum += y;
       mwi = fma(y, t.inv_mw[k], mwi);
+      W[k] = y;  // parked in the accumulator column until C is formed
     }
     const double yN = 1.0 - ysum;
     mwi = fma(yN, t.inv_mw[N - 1], mwi);
     const double rho = P / mwi * (s.invT * INV_RU);
     for (int k = 0; k < N - 1; ++k) {
-      C[k] = d2f_rn(b.Y[(int64_t)k * b.ld + i] * (rho * t.inv_mw[k]));
+      C[k] = d2f_rn(W[k] * (rho * t.inv_mw[k]));
       W[k] = 0.0;
     }
     C[N - 1] = d2f_rn(yN * (rho * t.inv_mw[N - 1]));
@@ -582,8 +604,10 @@ __global__ void __launch_bounds__(352, 1)
     kc.invT = s.invT;
     if constexpr (KC1) kc.Tbits = __double_as_longlong(s.T);
     Shapes<0, STAGES, KC>::run(t, s, C, kc, W, b, i);
-    for (int p = t.seg[NSHAPE]; p < t.R; ++p)
-      general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
+    for (int p = t.seg[NSHAPE]; p < t.seg[NSHAPE + 1]; ++p)
+      general<STAGES, false>(t, t.perm[p], s, mix, C, kc, W, b, i);
+    for (int p = t.seg[NSHAPE + 1]; p < t.R; ++p)  // PLOG / Chebyshev
+      general<STAGES, true>(t, t.perm[p], s, mix, C, kc, W, b, i);
     for (int k = 0; k < N; ++k) {
       const double v = W[k];
       bad += ((__double2hiint(v) >> 20) & 0x7ff) == 0x7ff;  // inf or NaN, integer test
@@ -591,6 +615,7 @@ __global__ void __launch_bounds__(352, 1)
     }
   }
   if (bad && b.status) atomicAdd(&b.status[1], bad);
+  sched_done(b.sched, amask, lane);
 }
 
 // ---- warp per state (see crs_fast.cu for the layout) --------------------
@@ -763,17 +788,18 @@ int grid_for(int64_t n, int block, int max_ctas);
 cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
                                   const Batch &b, int sm_count, int smem_optin,
                                   cudaStream_t s) {
+  const bool stages = b.conc || b.fwd || b.rev || b.pm;
+  auto k = L.kc_single ? (stages ? mixed::k_wdot<true, true> : mixed::k_wdot<false, true>)
+                       : (stages ? mixed::k_wdot<true, false> : mixed::k_wdot<false, false>);
   const size_t tab = (size_t)(L.rng[2][1] - L.rng[2][0] + L.rng[2][3] - L.rng[2][2]);
   const size_t per = (size_t)L.N * (8 + 4);
   const long long room = (long long)smem_optin - (long long)tab;
   // any thread count: a last partial warp still adds states in flight
   int block = room > 0 ? (int)(room / (long long)per) : 0;
   if (block > 352) block = 352;
-  if (block < 32) return cudaErrorNotSupported;
+  // the compact nu lists must be exact (else the warp kernel runs)
+  if (block < 32 || !L.nu_hi_exact) return cudaErrorNotSupported;
   const size_t bytes = tab + per * block;
-  const bool stages = b.conc || b.fwd || b.rev || b.pm;
-  auto k = L.kc_single ? (stages ? mixed::k_wdot<true, true> : mixed::k_wdot<false, true>)
-                       : (stages ? mixed::k_wdot<true, false> : mixed::k_wdot<false, false>);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
   return cudaGetLastError();
