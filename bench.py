@@ -150,8 +150,9 @@ class Clocks(object):
                 "samples": len(rows)}
 
 
-def _traffic_from_profiles(kernel):
-    """DRAM bytes per state from the committed ncu summary, if any."""
+def _profile_value(key, kernel):
+    """A per-state figure (`key[kernel]: value` line) from the committed ncu
+    summaries, if any."""
     d = os.path.join(HERE, "profiles")
     if not os.path.isdir(d):
         return None
@@ -160,11 +161,31 @@ def _traffic_from_profiles(kernel):
             continue
         with open(os.path.join(d, fn)) as f:
             txt = f.read()
-        m = re.search(r"^dram_bytes_per_state\[%s\]:\s*([0-9.eE+-]+)" % re.escape(kernel),
+        m = re.search(r"^%s\[%s\]:\s*([0-9.eE+-]+)" % (re.escape(key), re.escape(kernel)),
                       txt, re.M)
         if m:
             return float(m.group(1))
     return None
+
+
+def _traffic_from_profiles(kernel):
+    """DRAM bytes per state from the committed ncu summary, if any."""
+    return _profile_value("dram_bytes_per_state", kernel)
+
+
+def _fp64_pipe(kernel, states_per_s, peaks):
+    """FP64-pipe view of a kernel: FP64 instructions per state (DFMA + DADD +
+    DMUL, counted by ncu) x states/s against the measured FP64 issue rate."""
+    ops = _profile_value("fp64_ops_per_state", kernel)
+    if ops is None:
+        return None
+    achieved = ops * states_per_s
+    return {"ops_per_state": ops, "achieved_gops": achieved / 1e9,
+            "peak_gops": peaks["fp64_fma_ops"] / 1e9,
+            "frac": achieved / peaks["fp64_fma_ops"],
+            "source": "FP64 instructions per state from the ncu capture in "
+                      "profiles/wdot_kernels_gri53_262144_states.md; peak = FP64 FMA "
+                      "issue rate measured in-run (crs_probe_peaks)"}
 
 
 def run_reference(args):
@@ -309,7 +330,8 @@ def run_ours(args):
                                  max(2, args.steps // 2), 1, stream, dist)
         mixed = {"states": nm, "value": nm * world / (msm * 1e-3), "unit": "states/s",
                  "ms_per_step": msm, "plain_fp64_same_size": nm * world / (ms_plain22 * 1e-3),
-                 "speedup_vs_plain": ms_plain22 / msm, "error_vs_fp64": accuracy["mixed"]}
+                 "speedup_vs_plain": ms_plain22 / msm, "error_vs_fp64": accuracy["mixed"],
+                 "fp64_pipe": _fp64_pipe("mixed", nm / (msm * 1e-3), peaks)}
         del mT, mP, mY, mo
 
     # the ODE right-hand side around wdot (dydt, rate_subs.py:1829-2067)
@@ -404,7 +426,10 @@ def run_ours(args):
             "bound": "fp64", "unit": "GFLOP/s",
             "achieved": achieved / 1e9, "peak": peak / 1e9, "frac": achieved / peak,
             "peak_source": "measured in-run: FP64 FMA issue rate and CUDA exp() rate "
-                           "(crs_probe_peaks); transcendentals counted at exp()'s cost",
+                           "(crs_probe_peaks); transcendentals counted at exp()'s cost, "
+                           "which is why frac can exceed 1: the kernel's table-driven exp "
+                           "costs ~9 FP64 instructions; fp64_pipe is the executed view",
+            "fp64_pipe": _fp64_pipe("fp64", value / world, peaks),
             "per_state": {"flops": wk["flops"], "transcendentals": wk["transcendentals"],
                           "roofline_ns": t_roof * 1e9, "measured_ns": per_state_s * 1e9},
             "traffic": (traffic * n if traffic is not None else None),
