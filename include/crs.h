@@ -19,7 +19,11 @@
  *    the last failure of the calling thread;
  *  - a crs_mech is immutable after crs_mech_load and may be used from
  *    several host threads at once; each handle owns one device status word
- *    that concurrent launches on the same handle share.
+ *    that concurrent launches on the same handle share, and 256 scheduling
+ *    counters that its one-state-per-thread launches draw in turn: at most
+ *    256 such launches of one handle may be in flight at the same time
+ *    (several streams; a captured CUDA graph replayed on several streams at
+ *    once counts every replay).
  * Units are the reference's: T [K], P [Pa], C [kmol/m^3], rates
  * [kmol/(m^3 s)].
  */
@@ -49,7 +53,11 @@ typedef struct crs_mech crs_mech;
 #define CRS_MODE_MIXED 2       /* FP32 bulk, FP64 Kc exponent/net rate/sum */
 /* The arithmetic of CRS_MODE_FP64 / CRS_MODE_MIXED with a fixed thread
  * layout: one state per thread (TPS) or one state per warp (WARP).  The
- * default modes pick the faster layout that fits the mechanism. */
+ * default modes pick the faster layout that fits the mechanism.
+ * CRS_MODE_MIXED_TPS also needs every stoichiometric coefficient to be
+ * exact in 21 significant bits (integers, halves, ...); else, like a
+ * mechanism whose per-thread columns do not fit, it returns
+ * CRS_ERR_UNSUPPORTED and CRS_MODE_MIXED runs the warp layout. */
 #define CRS_MODE_FP64_TPS 3
 #define CRS_MODE_MIXED_TPS 4
 #define CRS_MODE_FP64_WARP 5
