@@ -510,6 +510,7 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     sur.features(Te, Pe, Ye, ne, ne, X, box=False)
     Yh = torch.empty((ne, net.pad[-1]), dtype=torch.float32, device="cuda")
     ms_fwd = _time_steps(lambda: net.forward(X, ne, Yh), 5, 2, stream, dist)
+    ms_inf = _time_steps(lambda: net.infer(X, ne, Yh), 5, 2, stream, dist)
     del X, Yh
     # error of the gated result and of the raw network, on every state
     rs.wdot(Te, Pe, Ye, "fp64", out=exact)
@@ -547,6 +548,8 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
         pass
     peak = peak or 1900.0
     fwd_tflops = 2.0 * macs * ne / (ms_fwd * 1e-3) / 1e12
+    inf_tflops = 2.0 * macs * ne / (ms_inf * 1e-3) / 1e12
+    fused = net.fused_ok()
     res = {
         "network": "MLP %s, SiLU, bf16 weights / fp32 accumulation, tcgen05 GEMMs"
                    % "->".join(str(d) for d in net.dims),
@@ -568,10 +571,15 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
         "error_gated": err_gated, "error_network_all_states": err_raw,
         "error_network_served_states": err_served,
         "gate_sweep": sweep,
-        "roofline": {"bound": "tensor", "kernel": "network forward (4 tcgen05 GEMMs + "
-                     "epilogues)", "achieved": fwd_tflops, "peak": peak, "unit": "TFLOP/s",
-                     "frac": fwd_tflops / peak, "flops_per_state": 2 * macs,
-                     "peak_note": "bf16 burst, of measured"},
+        "roofline": {"bound": "tensor",
+                     "kernel": ("network inference, all layers in one kernel (crs_mlp_infer)"
+                                if fused else "network forward, one tcgen05 GEMM per layer"),
+                     "achieved": inf_tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": inf_tflops / peak, "flops_per_state": 2 * macs,
+                     "peak_note": "bf16 burst, of measured",
+                     "layer_by_layer": {"achieved": fwd_tflops, "frac": fwd_tflops / peak,
+                                        "ms": ms_fwd},
+                     "fused_ms": ms_inf},
     }
     del Te, Pe, Ye, out, exact, w, raw, den, e_raw, served, wt
     return res

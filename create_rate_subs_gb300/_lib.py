@@ -58,6 +58,7 @@ def _sig(lib):
         "crs_gemm_bf16": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp],
         "crs_mlp_forward": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _i32, _vp, _i64,
                             _vp, _i64, _vp, _i64, _vp, _i64, _vp],
+        "crs_mlp_infer": [_vp, _i64, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_mlp_backward_data": [_vp, _vp, _i64, _i64, _i64, _i64, _i64, _vp, _i64, _vp,
                                   _i64, _vp, _i64, _vp],
         "crs_mlp_backward_weight": [_vp, _vp, _i64, _i64, _i64, _i64, _i64, _i32, _vp, _vp,

@@ -186,6 +186,32 @@ class MLP(object):
             a = out
         return Y
 
+    def fused_ok(self):
+        """True when infer() runs the whole network in one kernel: at most
+        6 layers, every padded width <= 256."""
+        return self.L <= 6 and max(self.pad) <= 256
+
+    def infer(self, X, m, Y, stream=None):
+        """forward() for inference: the whole network in one kernel per tile
+        of 128 states (crs_mlp_infer), the activations kept on chip, when
+        fused_ok(); the layer-by-layer forward() otherwise.  Same arguments
+        and result."""
+        if not self.fused_ok():
+            return self.forward(X, m, Y, stream)
+        s = stream if stream is not None else _stream(self.device)
+        M_pad = X.shape[0]
+        if M_pad % 128 or M_pad < m or X.shape[1] != self.pad[0] or not X.is_contiguous():
+            raise ValueError("X must be a contiguous (m rounded up to 128, %d)" % self.pad[0])
+        if Y.dim() != 2 or Y.shape[0] < m or Y.shape[1] < self.dims[-1] or Y.stride(1) != 1:
+            raise ValueError("Y must be (m, >= %d) with unit column stride" % self.dims[-1])
+        L = self.L
+        args = (ctypes.c_int64 * (L + 1))(*self.dims), (ctypes.c_int64 * (L + 1))(*self.pad), \
+            (ctypes.c_void_p * L)(*[w.data_ptr() for w in self.W]), \
+            (ctypes.c_void_p * L)(*[b.data_ptr() for b in self.b32])
+        _lib.check(self.lib.crs_mlp_infer(_p(X), M_pad, m, L, *args, _p(Y), Y.stride(0),
+                                          None, s))
+        return Y
+
     def train_step(self, X, XT, Tg, lr, loss_slot=None, splits=32, b1=0.9, b2=0.999,
                    eps=1e-8, stream=None):
         """One Adam step on the batch (X: bf16 (M, pad[0]), XT: bf16
@@ -394,7 +420,7 @@ class Surrogate(object):
         X = torch.zeros((M, self.net.pad[0]), dtype=torch.bfloat16, device=self.device)
         self.features(T, P, Y, Y.stride(0), n, X, box=False)
         Yh = torch.empty((n, self.net.pad[-1]), dtype=torch.float32, device=self.device)
-        self.net.forward(X, n, Yh)
+        self.net.infer(X, n, Yh)
         return Yh[:, : self.N]
 
     # -- evaluation ------------------------------------------------------
@@ -418,7 +444,7 @@ class Surrogate(object):
         flag = torch.empty(n, **u8)
         self.features(T, P, Y, ld, n, X, out_of_box=box)
         Yh = torch.empty((n, self.net.pad[-1]), dtype=torch.float32, device=self.device)
-        self.net.forward(X, n, Yh, s)
+        self.net.infer(X, n, Yh, s)
         _lib.check(self.lib.crs_surrogate_output(
             n, _p(Yh), Yh.stride(0), N, _p(self._scale_m), _p(self._scale_e), _p(self._cons), self.n_elem,
             tol, _p(box), _p(out), n, _p(flag), s))

@@ -221,6 +221,18 @@ int crs_mlp_forward(const void *X, const void *W, const float *b,
                     int64_t N, int act, float *Z, int64_t ldz, void *A,
                     int64_t lda, void *AT, int64_t ldat, float *Y32,
                     int64_t ldy, void *stream);
+/* Inference through the whole network in one kernel: Y32[:M][:dims[L]]
+ * (fp32, row stride ldy) = layer L-1(... SiLU(layer 0(X))), X bf16
+ * [M_pad][pads[0]] (M_pad a multiple of 128).  Layer l: W[l] bf16
+ * [pads[l+1]][pads[l]] (zero outside dims), b[l] fp32 [dims[l+1]]; SiLU
+ * after every layer but the last.  1 <= L <= 6, every pads[l] a multiple of
+ * 64 and <= 256.  Each CTA keeps its 128 states' activations in shared
+ * memory between layers.  status (may be NULL): device int32[2], bit 2 of
+ * status[0] is set when a bounded device wait expires. */
+int crs_mlp_infer(const void *X, int64_t M_pad, int64_t M, int L,
+                  const int64_t *dims, const int64_t *pads, const void *const *W,
+                  const float *const *b, float *Y32, int64_t ldy, int32_t *status,
+                  void *stream);
 /* dZprev = (dZ[M_pad][Kout] WT[Nin_pad][Kout]^T) * silu'(Zprev): the
  * gradient through a layer's weights and the previous SiLU; written
  * row-major [M][ld] and transposed [Nin][ldt] (dZprevT may be NULL). */

@@ -70,6 +70,34 @@ def test_forward_layer_matches_torch():
     assert (A[:, n_valid:] == 0).all() and (A[m_valid:] == 0).all()
 
 
+@pytest.mark.parametrize("dims,m", [([55, 256, 256, 256, 53], 1000),
+                                    ([55, 64, 128, 53], 300),
+                                    ([55, 256, 53], 129),
+                                    ([130, 128, 64, 256, 40], 513)])
+def test_fused_inference_matches_layers(dims, m):
+    """crs_mlp_infer (all layers in one kernel, activations on chip) against
+    the layer-by-layer forward (activations through HBM) on the same bf16
+    operands: the same fp32 sums in the same order, the same epilogue."""
+    from create_rate_subs_gb300.surrogate import MLP
+    net = MLP(dims, seed=11)
+    assert net.fused_ok()
+    M = (m + 127) // 128 * 128
+    g = torch.Generator(device="cuda").manual_seed(5)
+    X = torch.zeros((M, net.pad[0]), dtype=torch.bfloat16, device="cuda")
+    X[:m, : dims[0]] = torch.randn((m, dims[0]), generator=g, device="cuda").to(torch.bfloat16)
+    ref = torch.full((m, net.pad[-1]), float("nan"), device="cuda")
+    got = torch.full((m, net.pad[-1]), float("nan"), device="cuda")
+    net.forward(X, m, ref)
+    net.infer(X, m, got)
+    torch.cuda.synchronize()
+    n = dims[-1]
+    assert torch.isfinite(got[:, :n]).all()
+    assert torch.isnan(got[:, n:]).all()          # columns past the output untouched
+    err = float(((got[:, :n] - ref[:, :n]).abs().max() / ref[:, :n].abs().max()))
+    print(dims, "max diff / max |y| =", err)
+    assert err <= 1e-6
+
+
 def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
