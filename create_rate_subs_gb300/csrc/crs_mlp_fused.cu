@@ -92,6 +92,20 @@ __device__ __forceinline__ void ld32_nw(uint32_t taddr, uint32_t *v) {
       : "r"(taddr));
 }
 
+// tcgen05.wait::ld, then an empty asm that rewrites v: reads of v are
+// ordered after the wait (the registers of an outstanding TMEM load hold
+// garbage until then)
+__device__ __forceinline__ void wait_ld(uint32_t (&v)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  asm volatile(""
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]),
+                 "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]),
+                 "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]), "+r"(v[16]), "+r"(v[17]),
+                 "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]),
+                 "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]),
+                 "+r"(v[30]), "+r"(v[31]));
+}
+
 __device__ __forceinline__ void arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -204,17 +218,12 @@ __global__ void __launch_bounds__(NT, 2)
       const bool last = l == L - 1;
       const int nn = net.pad[l + 1], nv = net.dim[l + 1];
       const float4 *bias4 = reinterpret_cast<const float4 *>(sbias + l * MAXW);
-      // 64 columns (one K block of the next layer) per step: two TMEM loads
-      // in flight, one wait
-      for (int c = 0; c < nn; c += 64) {
-        uint32_t v[64];
-        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
-        ld32_nw(ta, v);
-        ld32_nw(ta + 32, v + 32);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        float z[64];
+      // bias, then the fp32 output (last layer) or SiLU -> bf16 into the
+      // activation buffer, for accumulator columns c .. c + 31 of the row
+      auto process = [&](const uint32_t(&v)[32], int c) {
+        float z[32];
 #pragma unroll
-        for (int t = 0; t < 16; ++t) {  // padded columns: 0 + 0 (zero weights and bias)
+        for (int t = 0; t < 8; ++t) {  // padded columns: 0 + 0 (zero weights and bias)
           const float4 b = bias4[(c >> 2) + t];
           z[4 * t] = __uint_as_float(v[4 * t]) + b.x;
           z[4 * t + 1] = __uint_as_float(v[4 * t + 1]) + b.y;
@@ -225,31 +234,46 @@ __global__ void __launch_bounds__(NT, 2)
           const int gr = m0 + row;
           if (gr < net.m_valid && c < nv) {
             float *y = net.Y + (int64_t)gr * net.ldy + c;
-            const int w = nv - c < 64 ? nv - c : 64;  // columns to write
+            const int w = nv - c < 32 ? nv - c : 32;  // columns to write
             const int nq = (reinterpret_cast<uintptr_t>(y) & 15) ? 0 : w >> 2;
 #pragma unroll
-            for (int t = 0; t < 16; ++t)
+            for (int t = 0; t < 8; ++t)
               if (t < nq)
                 reinterpret_cast<float4 *>(y)[t] =
                     make_float4(z[4 * t], z[4 * t + 1], z[4 * t + 2], z[4 * t + 3]);
 #pragma unroll
-            for (int j = 0; j < 64; ++j)
+            for (int j = 0; j < 32; ++j)
               if (j >= 4 * nq && j < w) y[j] = z[j];
           }
         } else {
-          // 64 bf16 = the row's eight 16-byte chunks of K block c / 64,
+          // 32 bf16 = four of the row's 16-byte chunks of K block c / 64,
           // swizzled: chunk j of row r sits at chunk j ^ (r % 8)
           unsigned char *blk = act + (c >> 6) * BLK + row * 128;
+          const int j0 = (c & 63) >> 3;
 #pragma unroll
-          for (int t = 0; t < 8; ++t) {
+          for (int t = 0; t < 4; ++t) {
             const float *a = z + 8 * t;
             const uint4 u = make_uint4(pack_bf16(silu(a[0]), silu(a[1])),
                                        pack_bf16(silu(a[2]), silu(a[3])),
                                        pack_bf16(silu(a[4]), silu(a[5])),
                                        pack_bf16(silu(a[6]), silu(a[7])));
-            *reinterpret_cast<uint4 *>(blk + ((t ^ (row & 7)) << 4)) = u;
+            *reinterpret_cast<uint4 *>(blk + (((j0 + t) ^ (row & 7)) << 4)) = u;
           }
         }
+      };
+      // two 32-column buffers: the TMEM load of the next columns is in
+      // flight while the current ones are processed
+      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
+      uint32_t va[32], vb[32];
+      ld32_nw(ta, va);
+      wait_ld(va);
+      for (int c = 0; c < nn; c += 64) {  // nn is a multiple of 64
+        ld32_nw(ta + (uint32_t)(c + 32), vb);
+        process(va, c);
+        wait_ld(vb);
+        if (c + 64 < nn) ld32_nw(ta + (uint32_t)(c + 64), va);
+        process(vb, c + 32);
+        wait_ld(va);
       }
       if (!last) {
         // generic-proxy stores -> visible to the tensor core's async proxy
