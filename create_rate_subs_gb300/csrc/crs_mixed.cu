@@ -732,11 +732,13 @@ __global__ void __launch_bounds__(DW * 32)
         }
       } else {
         // scale centre: mean binary exponent of the nonzero finite terms
+        // (tests on the bit pattern: no FP64 instruction)
         int esum = 0, ecnt = 0;
         for (int r = lane; r < R; r += 32) {
-          const double v = q[r];
-          if (v != 0.0 && isfinite(v)) {
-            esum += dexp2(v);
+          const int hi = __double2hiint(q[r]);
+          const int e = (hi >> 20) & 0x7ff;
+          if (e != 0x7ff && ((hi & 0x7fffffff) | __double2loint(q[r])) != 0) {
+            esum += e - 1023;
             ++ecnt;
           }
         }
@@ -746,29 +748,40 @@ __global__ void __launch_bounds__(DW * 32)
         const int c = ecnt ? (int)lrint((double)esum / ecnt) : 0;
         if (lane == 0) qo.escale[i] = c;
         __syncwarp();
-        const double sc = __hiloint2double((-c + 1023) << 20, 0);  // 2^-c
         __nv_bfloat16 *row = static_cast<__nv_bfloat16 *>(qo.A) + (int64_t)i * qo.lda;
+        bool any_out = false;
         for (int r = lane; r < qo.Kh; r += 32) {
-          double v = r < R ? q[r] : 0.0;
-          const bool inwin = v == 0.0 || (isfinite(v) && abs(dexp2(v) - c) <= WINDOW);
+          const double v = r < R ? q[r] : 0.0;
+          const int hi = __double2hiint(v), lo = __double2loint(v);
+          const int e = (hi >> 20) & 0x7ff;
+          // zero, or a normal number within WINDOW binary orders of c
+          const bool zero = ((hi & 0x7fffffff) | lo) == 0;
+          const bool inwin = zero || (e != 0 && e != 0x7ff && abs(e - 1023 - c) <= WINDOW);
+          float f = 0.0f;
           if (!inwin) {
             atomicOr(&mask[r >> 5], 1u << (r & 31));
-            v = 0.0;
+            any_out = true;
+          } else if (!zero) {
+            // v * 2^-c exactly, by the exponent field (the result stays a
+            // normal number within 2^+-WINDOW), then rounded to fp32
+            f = d2f_rn(__hiloint2double(hi - (c << 20), lo));
           }
-          const float f = (float)(v * sc);
-          const __nv_bfloat16 hi = __float2bfloat16_rn(f);
-          row[r] = hi;
-          row[qo.Kh + r] = __float2bfloat16_rn(f - __bfloat162float(hi));
+          const __nv_bfloat16 bh = __float2bfloat16_rn(f);
+          row[r] = bh;
+          row[qo.Kh + r] = __float2bfloat16_rn(f - __bfloat162float(bh));
         }
+        any_out = __any_sync(0xffffffffu, any_out);
         __syncwarp();
-        // out-of-window terms in FP64, in reaction order per species
+        // out-of-window terms in FP64, in reaction order per species (the
+        // contraction's epilogue adds the rest); zeros when there are none
         for (int a = l0; a < l1; ++a) {
           const int k = t.lane_sp[a];
           double w = 0.0;
-          for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e) {
-            const int r = t.spc_r[e];
-            if (mask[r >> 5] & (1u << (r & 31))) w = fma(t.spc_nu[e], q[r], w);
-          }
+          if (any_out)
+            for (int e = t.spc_ptr[k]; e < t.spc_ptr[k + 1]; ++e) {
+              const int r = t.spc_r[e];
+              if (mask[r >> 5] & (1u << (r & 31))) w = fma(t.spc_nu[e], q[r], w);
+            }
           b.wdot[(int64_t)k * b.ld + i] = w;
         }
       }
