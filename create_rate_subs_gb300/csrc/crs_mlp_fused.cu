@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 
 #include "../../include/crs.h"
 #include "crs_gemm.cuh"
@@ -304,6 +305,14 @@ __global__ void __launch_bounds__(NT, 2)
 }  // namespace mlpf
 }  // namespace crs
 
+namespace {
+int infer_error(int code, const char *what) {
+  char buf[200];
+  snprintf(buf, sizeof buf, "crs_mlp_infer: %s", what);
+  return crs::report(code, buf);
+}
+}  // namespace
+
 extern "C" int crs_mlp_infer(const void *X, int64_t M_pad, int64_t M, int L,
                              const int64_t *dims, const int64_t *pads, const void *const *W,
                              const float *const *b, float *Y32, int64_t ldy,
@@ -311,23 +320,25 @@ extern "C" int crs_mlp_infer(const void *X, int64_t M_pad, int64_t M, int L,
   using namespace crs;
   if (!X || !dims || !pads || !W || !b || !Y32 || L < 1 || L > mlpf::MAXL || M < 0 ||
       M > M_pad || M_pad % 128)
-    return CRS_ERR_ARG;
+    return infer_error(CRS_ERR_ARG, "null pointer, 1 <= L <= 6, or bad row counts "
+                                    "(M_pad a multiple of 128)");
   mlpf::Net net{};
   net.L = L;
   for (int l = 0; l <= L; ++l) {
     if (pads[l] < 64 || pads[l] > mlpf::MAXW || pads[l] % 64 || dims[l] < 1 || dims[l] > pads[l])
-      return CRS_ERR_ARG;
+      return infer_error(CRS_ERR_ARG, "widths must pad to multiples of 64 up to 256");
     net.pad[l] = (int)pads[l];
     net.dim[l] = (int)dims[l];
   }
-  if (ldy < dims[L]) return CRS_ERR_ARG;
+  if (ldy < dims[L]) return infer_error(CRS_ERR_ARG, "ldy < output width");
   if (M == 0) return CRS_OK;
   mlpf::Maps maps;
-  if (!make_tmap_bf16(&maps.x, X, M_pad, pads[0], 128)) return CRS_ERR_ARG;
+  if (!make_tmap_bf16(&maps.x, X, M_pad, pads[0], 128))
+    return infer_error(CRS_ERR_ARG, "X must be 16-byte aligned");
   for (int l = 0; l < L; ++l) {
-    if (!W[l] || !b[l]) return CRS_ERR_ARG;
     const int rows = pads[l + 1] < 128 ? (int)pads[l + 1] : 128;
-    if (!make_tmap_bf16(&maps.w[l], W[l], pads[l + 1], pads[l], rows)) return CRS_ERR_ARG;
+    if (!W[l] || !b[l] || !make_tmap_bf16(&maps.w[l], W[l], pads[l + 1], pads[l], rows))
+      return infer_error(CRS_ERR_ARG, "null or unaligned layer weights / bias");
     net.bias[l] = b[l];
   }
   net.m_valid = (int)M;
@@ -342,5 +353,5 @@ extern "C" int crs_mlp_infer(const void *X, int64_t M_pad, int64_t M, int L,
                         static_cast<cudaStream_t>(stream)>>>(maps, net);
     e = cudaGetLastError();
   }
-  return e == cudaSuccess ? CRS_OK : CRS_ERR_CUDA;
+  return e == cudaSuccess ? CRS_OK : infer_error(CRS_ERR_CUDA, cudaGetErrorString(e));
 }
