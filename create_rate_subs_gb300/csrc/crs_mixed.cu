@@ -764,7 +764,7 @@ __global__ void __launch_bounds__(DW * 32)
           } else if (!zero) {
             // v * 2^-c exactly, by the exponent field (the result stays a
             // normal number within 2^+-WINDOW), then rounded to fp32
-            f = d2f_rn(__hiloint2double(hi - (c << 20), lo));
+            f = d2f_rn(__hiloint2double(hi - c * (1 << 20), lo));
           }
           const __nv_bfloat16 bh = __float2bfloat16_rn(f);
           row[r] = bh;
