@@ -60,3 +60,27 @@ def test_per_state_call_without_binding_sets_error():
     out = (ctypes.c_double * 40)()
     lib.eval_rxn_rates(1000.0, 101325.0, out, out, out)
     assert "no mechanism bound" in _lib.last_error()
+
+
+@pytest.mark.parametrize("case", ["small", "gri53", "features", "features_lastAR"])
+def test_inspect_builds_every_table_image(case, golden):
+    """crs_mech_inspect builds the device table image on the host (every
+    blob section and derived table placed, the staged ranges inside the
+    image) for every golden mechanism, PLOG and Chebyshev included."""
+    mech, _ = golden(case)
+    lib = _lib.load()
+    out = (ctypes.c_int64 * 6)()
+    assert lib.crs_mech_inspect(mech.blob, len(mech.blob), out) == 0, _lib.last_error()
+    image, fp64_staged, mixed_staged = out[0], out[1], out[2]
+    assert image > 0 and 0 < fp64_staged <= image and 0 < mixed_staged <= image
+    assert image % 16 == 0
+
+
+def test_inspect_large_mechanism(synth_mech):
+    mech = synth_mech("large561")
+    lib = _lib.load()
+    out = (ctypes.c_int64 * 6)()
+    assert lib.crs_mech_inspect(mech.blob, len(mech.blob), out) == 0, _lib.last_error()
+    # the 561-species tables do not fit in shared memory: the warp kernels
+    # read them through L1 (the per-thread kernels are refused at launch)
+    assert out[0] > 227 * 1024
