@@ -80,16 +80,16 @@ def _config(n):
             "l2": "inputs larger than L2 (%d MB per step)" % (n * 856 // 2**20)}
 
 
-def _cpu_sample(mech, n_target, seconds=12.0, threads=0):
+def _cpu_sample(mech, n_target, seconds=12.0, threads=0, name=MECH, sample=1 << 16):
     """CPU baseline on a bounded sample: the reference's emitted C (OpenMP)
     when built, else the oracle port.  Returns dict for cpu_baseline."""
     from create_rate_subs_gb300 import synth
     from oracle.oracle import Oracle, RefLib
-    if RefLib.available(MECH, omp=True):
-        lib, kind = RefLib(MECH, omp=True), "reference"
+    if RefLib.available(name, omp=True):
+        lib, kind = RefLib(name, omp=True), "reference"
     else:
         lib, kind = Oracle(mech.blob), "port"
-    n = min(n_target, 1 << 16)
+    n = min(n_target, sample)
     T, P, Y = synth.make_states(mech.n_species, n, seed=777)
     lib.wdot_omp(T, P, Y, nthreads=threads)  # warm-up
     done, t0, used = 0, time.perf_counter(), 1
@@ -174,7 +174,7 @@ def _traffic_from_profiles(kernel):
 
 
 def _fp64_pipe(kernel, states_per_s, peaks):
-    """FP64-pipe view of a kernel: FP64 instructions per state (DFMA + DADD +
+    """Executed view of a kernel: FP64 instructions per state (DFMA + DADD +
     DMUL, counted by ncu) x states/s against the measured FP64 issue rate."""
     ops = _profile_value("fp64_ops_per_state", kernel)
     if ops is None:
@@ -186,6 +186,100 @@ def _fp64_pipe(kernel, states_per_s, peaks):
             "source": "FP64 instructions per state from the ncu capture in "
                       "profiles/wdot_kernels_gri53_262144_states.md; peak = FP64 FMA "
                       "issue rate measured in-run (crs_probe_peaks)"}
+
+
+def _peaks(lib):
+    """In-run issue-rate probes (include/crs_probe.h), operations/s."""
+    import ctypes
+    from create_rate_subs_gb300 import _lib
+    pk = (ctypes.c_double * 5)()
+    _lib.check(lib.crs_probe_peaks(pk))
+    return dict(fp64_fma_ops=pk[0], fp64_exp=pk[1], fp32_fma_ops=pk[2], sfu_ex2=pk[3],
+                fp64_table_exp=pk[4])
+
+
+def _measured_peak(key, fallback):
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            v = json.load(f).get(key)
+        if v:
+            return float(v), "of measured"
+    except (OSError, ValueError):
+        pass
+    return fallback, "of fallback"
+
+
+def _roofline(tables, precision, states_per_s, peaks, n_species, gemm=False):
+    """Roofline of one mode: the FP64-pipe work of the arithmetic the mode
+    keeps in FP64 (work.fp64_slots: a lower bound in FP64 instruction
+    slots, each transcendental priced at the measured cost of the table
+    exponential), the state bytes at the measured HBM bandwidth and, for
+    the tensor-core contraction, its flops at the measured bf16 peak.  The
+    bound is the slowest of them; frac = bound time / measured time."""
+    from create_rate_subs_gb300.work import contraction_flops, fp64_slots, state_bytes
+    exp_price = peaks["fp64_fma_ops"] / peaks["fp64_table_exp"]
+    sl = fp64_slots(tables, precision, exp_price)
+    t_fp64 = sl["slots"] / peaks["fp64_fma_ops"]
+    hbm, hbm_src = _measured_peak("hbm_gbs", 6800.0)
+    sb = state_bytes(n_species)
+    if gemm:
+        sb += 4 * int(tables["dims"][1])   # the bf16 hi+lo rate row, written once
+    t_hbm = sb / (hbm * 1e9)
+    t_meas = 1.0 / states_per_s
+    out = {"bound": "fp64", "unit": "GFLOP/s",
+           "achieved": 2 * sl["slots"] * states_per_s / 1e9,
+           "peak": 2 * peaks["fp64_fma_ops"] / 1e9,
+           "frac": t_fp64 / t_meas,
+           "fp64_slots_per_state": sl["slots"], "slots": sl["parts"],
+           "exp_price_slots": exp_price,
+           "peak_source": "FP64 FMA issue rate and the table exponential's rate, both "
+                          "measured in-run (crs_probe_peaks); one slot = one FP64 "
+                          "instruction = 2 flops",
+           "per_state_ns": {"fp64_bound": t_fp64 * 1e9, "hbm_bound": t_hbm * 1e9,
+                            "measured": t_meas * 1e9},
+           "hbm": {"achieved_gbs": sb * states_per_s / 1e9, "peak_gbs": hbm,
+                   "frac": sb * states_per_s / 1e9 / hbm, "peak_note": hbm_src,
+                   "algorithmic_bytes_per_state": sb}}
+    if gemm:
+        bf16, bsrc = _measured_peak("bf16_tflops_sustained", 1700.0)
+        fl = contraction_flops(tables)
+        t_tc = fl / (bf16 * 1e12)
+        out["tensor"] = {"flops_per_state": fl, "achieved_tflops": fl * states_per_s / 1e12,
+                         "peak_tflops": bf16, "peak_note": "bf16 sustained, " + bsrc,
+                         "frac": fl * states_per_s / 1e12 / bf16}
+        out["per_state_ns"]["tensor_bound"] = t_tc * 1e9
+    bound_t = max(v for k, v in out["per_state_ns"].items() if k != "measured") * 1e-9
+    out["bound"] = max((k for k in out["per_state_ns"] if k != "measured"),
+                       key=lambda k: out["per_state_ns"][k]).replace("_bound", "")
+    out["frac"] = bound_t / t_meas
+    return out
+
+
+def _ref_accuracy(name, mech, T, P, Y, results):
+    """Errors of GPU results against the reference's own emitted C for the
+    same states (oracle/_ref/<name>/libref.so, the parity build), or the
+    CPU oracle (bit-exact to it) when that build is absent.  T, P, Y, and
+    each result are host arrays; returns {mode: errors}."""
+    from oracle.oracle import Oracle, RefLib, gross_scale, wdot_errors
+    if RefLib.available(name):
+        lib, src = RefLib(name), "the reference's emitted C (oracle/_ref/%s/libref.so)" % name
+    else:
+        lib, src = Oracle(mech.blob), "the CPU oracle (bit-exact to the reference's C)"
+    ref = lib.eval(T, P, Y, want=("fwd", "rev", "pm", "wdot"))
+    G = gross_scale(mech.tables, ref["fwd"], ref["rev"], ref["pm"])
+    out = {}
+    for mode, w in results.items():
+        e = wdot_errors(w, ref["wdot"], G)
+        out[mode] = {"scaled_max": e["scaled"], "scaled_rms": e["scaled_rms"],
+                     "rel_max_1e-8G": e["rel_1e8"], "rel_max_1e-3G": e["rel_wellcond"],
+                     "states": int(T.shape[0]), "against": src}
+    return out
+
+
+ERROR_NOTE = ("scaled_max/rms: |w - w_ref| / G with G_k = sum_r |nu_kr| (|fwd_r| + "
+              "|rev_r|) pm_r (the survey's normalisation ii); rel_max_1e-8G: max "
+              "|w - w_ref| / |w_ref| over entries with |w_ref| >= 1e-8 G (normalisation "
+              "i), rel_max_1e-3G the same over |w_ref| >= 1e-3 G")
 
 
 def run_reference(args):
@@ -275,9 +369,7 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
 
     import ctypes
-    pk = (ctypes.c_double * 4)()
-    _lib.check(lib.crs_probe_peaks(pk))
-    peaks = dict(fp64_fma_ops=pk[0], fp64_exp=pk[1], fp32_fma_ops=pk[2], sfu_ex2=pk[3])
+    peaks = _peaks(lib)
 
     modes = {}
     for m in ("fp64", "fp64_strict", "mixed", "fp64_tps", "mixed_tps", "fp64_warp", "mixed_warp"):
@@ -309,13 +401,12 @@ def run_ours(args):
                   "note": "FP64 in the reference's own operation order (CUDA exp/log/pow, "
                           "divisions), same workload"}
 
-    # accuracy of each mode against the strict FP64 kernel on a sub-sample
-    sub = min(n, 1 << 15)
-    ref = rs.wdot_stages(dT[:sub], dP[:sub], dY[:, :sub], "fp64_strict")
-    accuracy = {}
-    for m in modes:
-        w = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], m)
-        accuracy[m] = _scaled_error(mech.tables, w, ref)
+    # accuracy of each mode against the reference's emitted C on a
+    # sub-sample of the timed states
+    sub = min(n, 1 << 16)
+    accuracy = _ref_accuracy(
+        MECH, mech, T[:sub], P[:sub], Y[:, :sub],
+        {m: rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], m).cpu().numpy() for m in modes})
 
     # mixed precision at 2^22 states
     mixed = None
@@ -328,11 +419,19 @@ def run_ours(args):
                           args.warmup, stream, dist)
         ms_plain22 = _time_steps(lambda: rs.wdot(mT, mP, mY, plain, out=mo),
                                  max(2, args.steps // 2), 1, stream, dist)
+        subm = 1 << 16
+        err22 = _ref_accuracy(
+            MECH, mech, T2[:subm], P2[:subm], Y2[:, :subm],
+            {"mixed": rs.wdot(mT[:subm], mP[:subm], mY[:, :subm], "mixed").cpu().numpy(),
+             plain: rs.wdot(mT[:subm], mP[:subm], mY[:, :subm], plain).cpu().numpy()})
         mixed = {"states": nm, "value": nm * world / (msm * 1e-3), "unit": "states/s",
                  "ms_per_step": msm, "plain_fp64_same_size": nm * world / (ms_plain22 * 1e-3),
-                 "speedup_vs_plain": ms_plain22 / msm, "error_vs_fp64": accuracy["mixed"],
+                 "speedup_vs_plain": ms_plain22 / msm,
+                 "error_vs_reference": err22["mixed"],
+                 "plain_error_vs_reference": err22[plain], "error_note": ERROR_NOTE,
+                 "roofline": _roofline(mech.tables, "mixed", nm / (msm * 1e-3), peaks, N),
                  "fp64_pipe": _fp64_pipe("mixed", nm / (msm * 1e-3), peaks)}
-        del mT, mP, mY, mo
+        del mT, mP, mY, mo, T2, P2, Y2
 
     # the ODE right-hand side around wdot (dydt, rate_subs.py:1829-2067)
     ydy = torch.cat([dT[None], dY], dim=0)
@@ -389,23 +488,13 @@ def run_ours(args):
     e2e_ok = bool(np.array_equal(hW[:, :4096].numpy(), out[:, :4096].cpu().numpy()))
 
     flags, bad = rs.status()
-    wk = work(mech.tables)
-    per_state_s = ms * 1e-3 / n
-    t_roof = wk["flops"] / (2 * peaks["fp64_fma_ops"]) + wk["transcendentals"] / peaks["fp64_exp"]
-    eq_flops = wk["flops"] + wk["transcendentals"] * (2 * peaks["fp64_fma_ops"] / peaks["fp64_exp"])
-    achieved = eq_flops / per_state_s
-    peak = 2 * peaks["fp64_fma_ops"]
-    sb = state_bytes(N)
-    hbm_peak = None
-    try:
-        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
-            hbm_peak = json.load(f).get("hbm_gbs")
-        hbm_src = "of measured"
-    except (OSError, ValueError):
-        pass
-    if hbm_peak is None:
-        hbm_peak, hbm_src = 6800.0, "of fallback"
     traffic = _traffic_from_profiles("fp64")
+    roof = _roofline(mech.tables, "fp64", value / world, peaks, N)
+    roof["traffic"] = traffic * n if traffic is not None else None
+    roof["traffic_note"] = ("DRAM bytes per launch: the per-state figure of the ncu capture "
+                            "in profiles/ (2^18 states) scaled to this launch's states")
+    roof["fp64_pipe"] = _fp64_pipe("fp64", value / world, peaks)
+    roof["per_state"] = work(mech.tables)
     line = {
         "metric": METRIC,
         "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
@@ -413,7 +502,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": _config(n), "plain_mode": plain, "fp64_strict": strict,
         "modes_states_per_s": per_mode,
-        "accuracy_vs_fp64_strict": accuracy,
+        "accuracy": accuracy, "accuracy_note": ERROR_NOTE,
         "mixed": mixed,
         "dydt": dydt_res,
         "e2e": {"value": n * world / (ms_e2e * 1e-3), "unit": "states/s",
@@ -422,21 +511,7 @@ def run_ours(args):
                 "path": "crs_wdot_host via ctypes: pinned host buffers, chunks of 2^17 "
                         "states on two streams, host clock around each call"},
         "gpu_launches": args.steps,
-        "roofline": {
-            "bound": "fp64", "unit": "GFLOP/s",
-            "achieved": achieved / 1e9, "peak": peak / 1e9, "frac": achieved / peak,
-            "peak_source": "measured in-run: FP64 FMA issue rate and CUDA exp() rate "
-                           "(crs_probe_peaks); transcendentals counted at exp()'s cost, "
-                           "which is why frac can exceed 1: the kernel's table-driven exp "
-                           "costs ~9 FP64 instructions; fp64_pipe is the executed view",
-            "fp64_pipe": _fp64_pipe("fp64", value / world, peaks),
-            "per_state": {"flops": wk["flops"], "transcendentals": wk["transcendentals"],
-                          "roofline_ns": t_roof * 1e9, "measured_ns": per_state_s * 1e9},
-            "traffic": (traffic * n if traffic is not None else None),
-            "hbm": {"achieved_gbs": sb / per_state_s / 1e9, "peak_gbs": hbm_peak,
-                    "frac": sb / per_state_s / 1e9 / hbm_peak, "peak_note": hbm_src,
-                    "algorithmic_bytes_per_state": sb},
-        },
+        "roofline": roof,
         "peaks_measured": {k: v / 1e9 for k, v in peaks.items()},
         "status": {"flags": flags, "nonfinite": bad},
         "clocks": clocks,
@@ -448,7 +523,7 @@ def run_ours(args):
         line["surrogate"] = _bench_surrogate(args, rs, stream, dist, world, rank)
         torch.cuda.empty_cache()
     if not args.no_large:
-        line["large_mechanism"] = _bench_large(args, stream, dist, world)
+        line["large_mechanism"] = _bench_large(args, stream, dist, world, peaks, rank)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_sample(mech, n_target=n, seconds=12.0)
     if rank == 0:
@@ -585,11 +660,12 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     return res
 
 
-def _bench_large(args, stream, dist, world):
+def _bench_large(args, stream, dist, world, peaks, rank):
     """Large-mechanism configuration: 561 species / 2539 reactions, 2^20
     states; CSR contraction on chip (fp64, mixed) vs the tensor-core
-    contraction (gemm); errors against fp64_strict on a sub-sample; the
-    contraction GEMM alone against the measured bf16 peak."""
+    contraction (gemm); errors against the reference's emitted C on a
+    sub-sample; a roofline per mode; the contraction GEMM alone against the
+    measured bf16 peak; the reference's C on the host cores beside it."""
     import ctypes
     import torch
     from create_rate_subs_gb300 import _lib, synth
@@ -603,19 +679,27 @@ def _bench_large(args, stream, dist, world):
     n = args.large_states
     T, P, Y = synth.make_states(N, n, seed=3000)
     dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[: N - 1].copy()))
-    del Y
     out = torch.empty((N, n), dtype=torch.float64, device="cuda")
     res = {"mechanism": "synthetic large561: 561 species / 2539 reactions "
                         "(254 three-body, 127 Troe, 156 irreversible)",
            "n_states": n, "modes": {}}
     sub = 4096
-    ref = rs.wdot_stages(dT[:sub], dP[:sub], dY[:, :sub], "fp64_strict")
+    steps = max(3, args.steps // 2)
+    got = {}
+    precision = {"fp64": "fp64", "mixed": "mixed", "gemm": "rates"}
     for mode in ("fp64", "mixed", "gemm"):
-        ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), 2, 1, stream, dist)
-        w = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], mode)
+        ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), steps, 2, stream, dist)
+        got[mode] = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], mode).cpu().numpy()
+        sps = n / (ms * 1e-3)
         res["modes"][mode] = {"value": n * world / (ms * 1e-3), "unit": "states/s",
-                              "ms_per_step": ms,
-                              "error_vs_fp64_strict": _scaled_error(mech.tables, w, ref)}
+                              "ms_per_step": ms, "timed_steps": steps,
+                              "roofline": _roofline(mech.tables, precision[mode], sps, peaks,
+                                                    N, gemm=(mode == "gemm"))}
+    acc = _ref_accuracy("large561", mech, T[:sub], P[:sub], Y[:, :sub], got)
+    for mode in got:
+        res["modes"][mode]["error_vs_reference"] = acc[mode]
+    res["error_note"] = ERROR_NOTE
+    del Y
     # the contraction GEMM alone, at one workspace chunk (2^18 states)
     lib = _lib.load()
     M, Kh = 1 << 18, (mech.n_reactions + 63) // 64 * 64
@@ -629,21 +713,18 @@ def _bench_large(args, stream, dist, world):
     ms = _time_steps(lambda: _lib.check(lib.crs_gemm_bf16(p(A), p(B), p(D), M, Np, K, Np, bn,
                                                           None, st)), 5, 2, stream, dist)
     flops = 2.0 * M * N * (2 * mech.n_reactions)
-    peak = None
-    try:
-        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
-            peak = json.load(f).get("bf16_tflops")
-    except (OSError, ValueError):
-        pass
-    peak = peak or 1900.0
+    peak, psrc = _measured_peak("bf16_tflops", 1900.0)
     res["contraction_gemm"] = {
         "shape": "M=%d states x N=%d species (padded %d) x K=2*%d (bf16 hi+lo, padded %d)"
                  % (M, N, Np, mech.n_reactions, K),
         "ms": ms, "achieved_tflops": flops / (ms * 1e-3) / 1e12, "peak_tflops": peak,
-        "frac": flops / (ms * 1e-3) / 1e12 / peak, "peak_note": "bf16 burst, of measured",
+        "frac": flops / (ms * 1e-3) / 1e12 / peak, "peak_note": "bf16 burst, " + psrc,
         "flops_note": "algorithmic 2*M*N*K on the unpadded sizes"}
     del A, B, D, out, dT, dP, dY
     torch.cuda.empty_cache()
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = _cpu_sample(mech, n_target=n, seconds=6.0, name="large561",
+                                          sample=1 << 12)
     return res
 
 
@@ -653,38 +734,6 @@ def _jsonable(o):
     if isinstance(o, (np.floating,)):
         return float(o)
     raise TypeError(type(o))
-
-
-def _scaled_error(tables, w, ref):
-        """Error of a wdot result against the strict FP64 kernel's stages."""
-        import torch
-        t = tables
-        fwd, rev, pm, wr = (ref[k].double() for k in ("fwd", "rev", "pm", "wdot"))
-        R = int(t["dims"][1])
-        N = int(t["dims"][0])
-        rev_idx = torch.as_tensor(t["rev_idx"], device=fwd.device, dtype=torch.long)
-        pm_idx = torch.as_tensor(t["pm_idx"], device=fwd.device, dtype=torch.long)
-        g = fwd.abs().clone()
-        has_rev = rev_idx >= 0
-        if rev.shape[0]:
-            g[has_rev] += rev.abs()[rev_idx[has_rev]]
-        has_pm = pm_idx >= 0
-        if pm.shape[0]:
-            g[has_pm] *= pm.abs()[pm_idx[has_pm]]
-        M = torch.zeros((N, R), dtype=torch.float64, device=fwd.device)
-        for r in range(R):
-            for e in range(t["nu_ptr"][r], t["nu_ptr"][r + 1]):
-                M[t["nu_sp"][e], r] += abs(float(t["nu_val"][e]))
-        G = M @ g
-        d = (w.double() - wr).abs()
-        zero = G == 0
-        s = torch.where(zero, d, d / torch.where(zero, torch.ones_like(G), G))
-        mask = (~zero) & (wr.abs() >= 1e-3 * G)
-        rel = (d[mask] / wr.abs()[mask]).max().item() if mask.any() else 0.0
-        return {"scaled_max": s.max().item(), "scaled_rms": s.pow(2).mean().sqrt().item(),
-                "rel_max_wellcond": rel,
-                "normalisation": "|w-w64|/G, G_k=sum_r |nu_kr|(|fwd_r|+|rev_r|)pm_r; "
-                                 "rel over |w64|>=1e-3 G"}
 
 
 def run_profile(args):

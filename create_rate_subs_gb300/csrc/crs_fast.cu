@@ -25,6 +25,7 @@
 
 #include <type_traits>
 
+#include "crs_exp.cuh"
 #include "crs_internal.cuh"
 #include "crs_shapes.cuh"
 
@@ -311,40 +312,12 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
 
 namespace fast {
 
-constexpr double INV_L = 369.3299304675746;     // 256 / ln 2
-constexpr double L_HI = 0x1.62e42fefa0000p-9;   // ln2/256, 35 bits
-constexpr double L_LO = 0x1.cf79abc9e3b3ap-48;  // ln2/256 - L_HI
-constexpr double SHIFT = 6755399441055744.0;    // 1.5 * 2^52
+using texp::exp_core;
+using texp::exp_fix;
+using texp::exp_t;
 constexpr double INV_RU = 0.0001202723625380408;
 constexpr double LN10 = 2.302585092994046;
 constexpr double INV_LN10 = 0.4342944819032518;
-
-// exp(x) from a 2^(j/256) table (see file comment), without the range
-// check: arguments beyond +-700 and NaN give garbage here and are replaced
-// by exp_fix.  The table index stays in [0, 255] for any input.
-__device__ __forceinline__ double exp_core(double x, const double *tab) {
-  const double t = fma(x, INV_L, SHIFT);
-  const double kd = t - SHIFT;
-  const int k = __double2loint(t);
-  double r = fma(kd, -L_HI, x);
-  r = fma(kd, -L_LO, r);
-  const double q = fma(fma(r, 1.0 / 24.0, 1.0 / 6.0), r, 0.5);
-  const double p = fma(q, r * r, r);
-  const double tj = tab[k & 255];
-  const int m = k >> 8;  // arithmetic shift: floor(k / 256)
-  const double s = __hiloint2double(__double2hiint(tj) + m * (1 << 20),
-                                    __double2loint(tj));
-  return fma(s, p, s);
-}
-// Overflow, underflow and NaN go to CUDA's exp.  |x| <= 700 is tested on
-// the high word as an integer (0x4085E000 = high word of 700.0; a larger
-// low word still leaves x below 700.0001): no FP64 instruction.
-__device__ __forceinline__ double exp_fix(double x, double e) {
-  return ((unsigned)__double2hiint(x) & 0x7fffffffu) <= 0x4085E000u ? e : exp(x);
-}
-__device__ __forceinline__ double exp_t(double x, const double *tab) {
-  return exp_fix(x, exp_core(x, tab));
-}
 
 struct Col {
   double *p;
@@ -869,7 +842,8 @@ cudaError_t launch_wdot_fp64_tps(const unsigned char *img, const ImgLayout &L,
   if (kcm == 0) k = stages ? fast::k_wdot<true, 0> : fast::k_wdot<false, 0>;
   else if (kcm == 1) k = stages ? fast::k_wdot<true, 1> : fast::k_wdot<false, 1>;
   else k = stages ? fast::k_wdot<true, 2> : fast::k_wdot<false, 2>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const cudaError_t e = set_smem_limit(k, bytes);
+  if (e != cudaSuccess) return e;
   k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
   return cudaGetLastError();
 }
@@ -894,9 +868,11 @@ cudaError_t launch_wdot_fp64(const unsigned char *img, const ImgLayout &L,
   const size_t bytes = (smem_tab ? tab : 0) + nw * pw;
   auto k = smem_tab ? (stages ? fast::k_wdot_warp<true, true> : fast::k_wdot_warp<false, true>)
                     : (stages ? fast::k_wdot_warp<true, false> : fast::k_wdot_warp<false, false>);
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = set_smem_limit(k, bytes);
+  if (e != cudaSuccess) return e;
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  if (e != cudaSuccess) return e;
   const int grid = grid_for(nbatch, nw, sm_count * (per_sm > 0 ? per_sm : 1));
   k<<<grid, nw * 32, bytes, s>>>(img, L, b, per_warp);
   return cudaGetLastError();

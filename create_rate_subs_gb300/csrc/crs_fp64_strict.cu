@@ -372,13 +372,13 @@ cudaError_t launch_wdot_strict(const unsigned char *img, const ImgLayout &L,
   const int grid = grid_for(b.n, block, sm_count * ctas_per_sm);
   if (tab + cols <= (size_t)smem_optin) {
     auto k = strict::k_wdot<true, true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(tab + cols));
+    const cudaError_t e = set_smem_limit(k, tab + cols);
+    if (e != cudaSuccess) return e;
     k<<<grid, block, tab + cols, s>>>(img, L, b);
   } else if (tab <= (size_t)smem_optin) {
     auto k = strict::k_wdot<true, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tab);
+    const cudaError_t e = set_smem_limit(k, tab);
+    if (e != cudaSuccess) return e;
     k<<<sm_count * 4 < grid ? sm_count * 4 : grid, block, tab, s>>>(img, L, b);
   } else {
     auto k = strict::k_wdot<false, false>;

@@ -441,4 +441,13 @@ struct KcPolyG {
 // Sets the text returned by crs_last_error() and returns code.
 int report(int code, const char *msg);
 
+#ifdef __CUDACC__
+// Raise kernel k's dynamic shared-memory limit to `bytes`.  Every launcher
+// returns this error instead of launching when the limit was not applied.
+template <class K>
+inline cudaError_t set_smem_limit(K k, size_t bytes) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+#endif
+
 }  // namespace crs

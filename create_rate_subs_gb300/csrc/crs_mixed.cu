@@ -813,7 +813,8 @@ cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
   // the compact nu lists must be exact (else the warp kernel runs)
   if (block < 32 || !L.nu_hi_exact) return cudaErrorNotSupported;
   const size_t bytes = tab + per * block;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const cudaError_t e = set_smem_limit(k, bytes);
+  if (e != cudaSuccess) return e;
   k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
   return cudaGetLastError();
 }
@@ -844,9 +845,11 @@ cudaError_t launch_wdot_mixed_q(const unsigned char *img, const ImgLayout &L,
                                      : mixed::k_wdot_warp<false, true, false>)
                            : (stages ? mixed::k_wdot_warp<true, false, false>
                                      : mixed::k_wdot_warp<false, false, false>);
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = set_smem_limit(k, bytes);
+  if (e != cudaSuccess) return e;
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nw * 32, bytes);
+  if (e != cudaSuccess) return e;
   const int grid = grid_for(nbatch, nw, sm_count * (per_sm > 0 ? per_sm : 1));
   k<<<grid, nw * 32, bytes, s>>>(img, L, b, per_warp, qo);
   return cudaGetLastError();

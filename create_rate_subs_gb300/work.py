@@ -6,12 +6,19 @@ rates.  ``work``: floating-point operations and transcendental calls that
 the reference's emitted C performs for one state (rate_subs.py:283-1391):
 eval_conc, eval_rxn_rates, get_rxn_pres_mod, eval_spec_rates.  An FMA
 counts 2 flops, a divide 1, a call to exp/log/log10/pow one transcendental.
+
+``fp64_slots``: the FP64-pipe work of one state as a count of FP64
+instruction slots, a lower bound for any implementation of the same
+arithmetic at the given precision split, so that slots x states/s over
+the measured FP64 issue rate cannot exceed 1 unless a kernel skips work.
+``contraction_flops``: the tensor-core work of the stoichiometric
+contraction of CRS_MODE_GEMM.
 """
 
 from .tables import (FORM_SRI, FORM_TROE, PM_THD, RATE_CONST, RATE_EXP,
                      RATE_NEGEXP, RATE_POW)
 
-__all__ = ["state_bytes", "work"]
+__all__ = ["state_bytes", "work", "fp64_slots", "contraction_flops"]
 
 
 def state_bytes(n_species, elem_bytes=8):
@@ -86,3 +93,51 @@ def work(tables):
             trans += 2 + 2 + 1 + de        # exps, 2 log10, pow, pow(T, e)
         flops += 3
     return dict(flops=int(flops), transcendentals=int(trans))
+
+
+def fp64_slots(tables, precision, exp_slots):
+    """FP64 instruction slots of one state.
+
+    precision "fp64": every operation of the emitted code in FP64.  The
+        algebraic flops count at most two per instruction (as if every
+        multiply fused with an add) and each transcendental at
+        ``exp_slots``, the measured FP64-pipe cost of the cheapest FP64
+        exponential of this library (the table exp: FP64 FMA rate / its
+        rate, ~9); logs and powers cost more, so this undercounts.
+    precision "mixed": only what the mixed split keeps in FP64 (the
+        equilibrium-constant exponent, the forward - reverse subtraction,
+        the wdot accumulation): 6 FMAs per Kc polynomial (per T_common
+        group), one subtraction per reversible reaction, one multiply per
+        reaction with a pres_mod term, one FMA per nonzero net
+        stoichiometric coefficient.
+    precision "rates": the mixed split without the accumulation (the rates
+        producer of the tensor-core contraction, whose products and sums
+        run on the tensor cores).
+    Returns dict(slots=..., parts={...}).
+    """
+    t = tables
+    R = int(t["dims"][1])
+    NREV = int(t["dims"][2])
+    groups = int(t["kc_ptr"][NREV]) if NREV else 0
+    nnz = int(t["nu_ptr"][R])
+    n_pm = int(sum(1 for r in range(R) if int(t["pm_idx"][r]) >= 0))
+    if precision == "fp64":
+        w = work(t)
+        parts = {"algebraic": w["flops"] / 2.0,
+                 "transcendental": w["transcendentals"] * float(exp_slots)}
+    elif precision in ("mixed", "rates"):
+        parts = {"kc_exponent": 6.0 * groups, "net_rate": float(NREV),
+                 "pres_mod_product": float(n_pm)}
+        if precision == "mixed":
+            parts["accumulation"] = float(nnz)
+    else:
+        raise ValueError("precision must be fp64, mixed or rates")
+    return {"slots": float(sum(parts.values())), "parts": parts}
+
+
+def contraction_flops(tables):
+    """Tensor-core flops of one state in CRS_MODE_GEMM: the rate row split
+    into bf16 hi + lo times the (R x N) stoichiometric matrix,
+    2 * 2R * N."""
+    N, R = int(tables["dims"][0]), int(tables["dims"][1])
+    return 4.0 * R * N

@@ -305,13 +305,6 @@ int crs_scatter_wdot(int64_t m, const int64_t *idx, const double *Wc,
                      int64_t ldc, int rows, double *W, int64_t ld,
                      void *stream);
 
-/* ---- measurement helper (no counterpart in the reference) ------------- */
-
-/* Issue-rate probes of the current device, operations per second:
- * out[0] FP64 FMA, out[1] CUDA double exp(), out[2] FP32 FMA, out[3] SFU
- * ex2.approx.  The roofline denominators of the FP64 and mixed kernels. */
-int crs_probe_peaks(double out[4]);
-
 /* ---- per-state drop-in (the reference's emitted signatures) ----------- */
 
 /* Select the mechanism used by the four functions below (NULL unbinds).

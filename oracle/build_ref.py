@@ -2,7 +2,8 @@
 
 Recipe, two steps:
 
-``generate``  (needs the reference checkout, default /root/reference)
+``generate``  (needs the reference checkout: the directory named by the
+    environment variable CRS_REFERENCE, default /root/reference)
     Copies the reference's five Python modules into a scratch directory,
     applies the minimal Python 3 patch (``except Exception, e`` ->
     ``as e`` and ``iteritems`` in chem_utilities.py; ``range`` ->
@@ -15,8 +16,8 @@ Recipe, two steps:
 
 ``compile``  (needs only ``oracle/_ref/<name>/`` and ``oracle/ref_harness.c``)
     Compiles the emitted files with the batch driver into
-    ``oracle/_ref/<name>/libref.so`` (``-O2 -ffp-contract=off``: the parity
-    build) and ``libref_omp.so`` (``-O3 -fopenmp``: the timed CPU baseline),
+    ``oracle/_ref/<name>/libref.so`` (``-O2 -ffp-contract=off -fopenmp``:
+    the parity build, states spread over threads) and ``libref_omp.so`` (``-O3 -fopenmp``: the timed CPU baseline),
     and the emitted ``dydt.c`` (constant pressure, ``-DCONP``) with
     ``ref_dydt_harness.c`` into ``libref_dydt.so``.
 
@@ -24,6 +25,7 @@ Recipe, two steps:
 working tree so that ``compile`` can run on another host.
 
 Usage: python oracle/build_ref.py {generate,compile,all} NAME [NAME ...]
+       python oracle/build_ref.py available   (exit 0 when the checkout exists)
        (NAME is a key of create_rate_subs_gb300.synth.CONFIGS)
 """
 
@@ -37,6 +39,8 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REF_OUT = os.path.join(HERE, "_ref")
+# The reference checkout that ``generate`` reads (never written).
+REFERENCE = os.environ.get("CRS_REFERENCE", "/root/reference")
 EMITTED = ("chem_utils.c", "rxn_rates.c", "rxn_rates_pres_mod.c",
            "spec_rates.c", "header.h", "rates.h", "chem_utils.h", "dydt.c",
            "dydt.h")
@@ -56,9 +60,9 @@ def ref_dir(name):
     return os.path.join(REF_OUT, name)
 
 
-def generate(name, mech_path, therm_path, reference="/root/reference",
-             last_spec=None):
+def generate(name, mech_path, therm_path, reference=None, last_spec=None):
     """Emit the reference's C for one mechanism into oracle/_ref/<name>/."""
+    reference = reference or REFERENCE
     if not os.path.isdir(reference):
         raise FileNotFoundError("reference checkout not found: " + reference)
     mech_path = os.path.abspath(mech_path)
@@ -147,7 +151,9 @@ def compile_ref(name, opt_parity=None, opt_fast=None):
     defs = ["-DCRS_NSP=%d" % nsp, "-DCRS_NR=%d" % nr,
             "-DCRS_NREV=%d" % nrev, "-DCRS_NPM=%d" % npm]
     base = ["gcc", "-shared", "-fPIC", "-I", d] + defs
-    jobs = [(base + [opt_parity, "-ffp-contract=off", "-o", "libref.so"]
+    # the parity build evaluates states on OpenMP threads (per-state
+    # arithmetic unchanged), so that tests can pin millions of states
+    jobs = [(base + [opt_parity, "-ffp-contract=off", "-fopenmp", "-o", "libref.so"]
              + srcs + [harness, "-lm"]),
             (base + [opt_fast, "-fopenmp", "-o", "libref_omp.so"]
              + srcs + [harness, "-lm"])]
@@ -173,7 +179,14 @@ def have_sources(name):
                          "header.h"))
 
 
+def reference_available():
+    """True when the reference checkout that ``generate`` reads exists."""
+    return os.path.isdir(REFERENCE)
+
+
 def main(argv):
+    if len(argv) == 2 and argv[1] == "available":
+        return 0 if reference_available() else 1
     if len(argv) < 3 or argv[1] not in ("generate", "compile", "all"):
         print(__doc__)
         return 2

@@ -221,24 +221,36 @@ class RefDydt(object):
         return misc, conc
 
 
-def gross_scale(blob_tables, fwd, rev, pm):
+def nu_abs_matrix(blob_tables):
+    """Dense (N, R) matrix of |nu_kr|, the net stoichiometric coefficients
+    of the tables' species-rate lists (rate_subs.py:1183-1216)."""
+    t = blob_tables
+    N, R = int(t["dims"][0]), int(t["dims"][1])
+    M = np.zeros((N, R))
+    ptr, sp, val = t["nu_ptr"], t["nu_sp"], t["nu_val"]
+    for r in range(R):
+        for e in range(ptr[r], ptr[r + 1]):
+            M[sp[e], r] += abs(val[e])
+    return M
+
+
+def gross_scale(blob_tables, fwd, rev, pm, nu_abs=None):
     """G[k, i] = sum_r |nu_kr| (|fwd_r| + |rev_r|) * pm_r: the scale of the
     terms summed into wdot_k, used to normalise errors where fwd and rev
-    cancel."""
+    cancel.  nu_abs: nu_abs_matrix(blob_tables), when the caller keeps it."""
     t = blob_tables
-    N = int(t["dims"][0])
     R = int(t["dims"][1])
-    n = fwd.shape[1]
-    G = np.zeros((N, n))
-    for r in range(R):
-        j = t["rev_idx"][r]
-        p = t["pm_idx"][r]
-        g = np.abs(fwd[r]) + (np.abs(rev[j]) if j >= 0 else 0.0)
-        if p >= 0:
-            g = g * np.abs(pm[p])
-        for e in range(t["nu_ptr"][r], t["nu_ptr"][r + 1]):
-            G[t["nu_sp"][e]] += abs(t["nu_val"][e]) * g
-    return G
+    rev_idx = np.asarray(t["rev_idx"][:R])
+    pm_idx = np.asarray(t["pm_idx"][:R])
+    g = np.abs(fwd)
+    has_rev = rev_idx >= 0
+    if np.any(has_rev):
+        g[has_rev] += np.abs(rev[rev_idx[has_rev]])
+    has_pm = pm_idx >= 0
+    if np.any(has_pm):
+        g[has_pm] *= np.abs(pm[pm_idx[has_pm]])
+    M = nu_abs if nu_abs is not None else nu_abs_matrix(t)
+    return M @ g
 
 
 def wdot_errors(w, w_ref, G):

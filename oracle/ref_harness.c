@@ -83,11 +83,16 @@ static void one_state(int64_t i, const double* T, const double* P,
   }
 }
 
-/* All stages for n states, serial. */
+/* All stages for n states.  States are independent and each is evaluated
+ * by the same per-state calls, so an OpenMP build (the parity build is one)
+ * spreads them over threads without changing any result. */
 int ref_eval(int64_t n, const double* T, const double* P, const double* Y,
              int64_t ld, double* conc, double* fwd, double* rev, double* pm,
              double* wdot, double* misc) {
   if (n < 0 || ld < n) return 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
   for (int64_t i = 0; i < n; ++i)
     one_state(i, T, P, Y, ld, conc, fwd, rev, pm, wdot, misc);
   return 0;

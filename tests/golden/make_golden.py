@@ -10,8 +10,9 @@ utilities (eval_h/u/cv/cp, eval_conc_rho) and the constant-pressure dydt
 <case>.npz together with the mechanism text, so that the tests can pin the
 front end and the oracle without the reference checkout.
 
-Run from the repository root:  python tests/golden/make_golden.py
-(needs the reference checkout at /root/reference).
+Run from the repository root:  python tests/golden/make_golden.py [CASE ...]
+(needs the reference checkout; oracle/build_ref.py says where it is looked
+for and how to point elsewhere).
 """
 
 import os
@@ -30,7 +31,8 @@ from oracle.oracle import RefDydt, RefLib  # noqa: E402
 
 # case -> (mechanism source, last_spec, n random states, state seed)
 CASES = {
-    "small": ("small", None, 256, 11),
+    # the small configuration's 1024 seeded states (+ the edge states)
+    "small": ("small", None, 1024, 11),
     "gri53": ("gri53", None, 48, 12),
     "features": ("features", None, 64, 13),
     "features_lastAR": ("features", "AR", 32, 14),

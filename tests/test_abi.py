@@ -1,6 +1,8 @@
-"""libcrs: it builds, loads, exports every symbol of include/crs.h and
-rejects bad input before touching a GPU (CPU only)."""
+"""libcrs: it builds, loads, exports every symbol that the C headers in
+include/ (*.h) declare and rejects bad input before touching a GPU (CPU
+only)."""
 import ctypes
+import glob
 import os
 import re
 
@@ -10,15 +12,20 @@ from conftest import REPO
 from create_rate_subs_gb300 import _lib, tables
 
 
-def header_functions():
-    with open(os.path.join(REPO, "include", "crs.h")) as f:
-        text = f.read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text)) - {"defined"})
+def header_functions(name=None):
+    paths = ([os.path.join(REPO, "include", name)] if name
+             else sorted(glob.glob(os.path.join(REPO, "include", "*.h"))))
+    fns = set()
+    for p in paths:
+        with open(p) as f:
+            text = f.read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        fns |= set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text)) - {"defined"}
+    return sorted(fns)
 
 
 def test_header_lists_the_reference_signatures():
-    fns = header_functions()
+    fns = header_functions("crs.h")
     for name in ("eval_conc", "eval_rxn_rates", "get_rxn_pres_mod",
                  "eval_spec_rates", "crs_wdot", "crs_mech_load"):
         assert name in fns
@@ -26,7 +33,9 @@ def test_header_lists_the_reference_signatures():
 
 def test_library_exports_every_header_symbol():
     lib = _lib.load()
-    missing = [f for f in header_functions() if not hasattr(lib, f)]
+    fns = header_functions()
+    assert "crs_probe_peaks" in fns          # include/crs_probe.h is read too
+    missing = [f for f in fns if not hasattr(lib, f)]
     assert not missing, missing
 
 

@@ -21,12 +21,15 @@ def test_oracle_bitexact_vs_golden(case, golden):
         assert np.array_equal(out[k], g[k]), k
 
 
-@pytest.mark.parametrize("name", ["small", "gri53"])
-def test_oracle_bitexact_vs_reference_build(name, synth_mech):
+@pytest.mark.parametrize("name,n", [("small", 3000), ("gri53", 3000), ("large561", 1024)])
+def test_oracle_bitexact_vs_reference_build(name, n, synth_mech):
+    """Every stage of the oracle equals the reference's own emitted C on
+    fresh seeded states, for each workload mechanism (the 561-species /
+    2539-reaction one included)."""
     if not RefLib.available(name):
         pytest.skip("reference C not built here (python oracle/build_ref.py all %s)" % name)
     mech = synth_mech(name)
-    T, P, Y = synth.make_states(mech.n_species, 3000, seed=99)
+    T, P, Y = synth.make_states(mech.n_species, n, seed=99)
     a = Oracle(mech.blob).eval(T, P, Y)
     b = RefLib(name).eval(T, P, Y)
     for k in a:
