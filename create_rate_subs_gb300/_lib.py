@@ -54,6 +54,19 @@ def _sig(lib):
         "crs_wdot_stages": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                             _vp, _i32, _vp],
         "crs_bind": [_vp],
+        "crs_bind_thread": [_vp],
+        "crs_mech_load_host": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
+        "crs_mech_image": [ctypes.c_char_p, ctypes.c_size_t, _vp, ctypes.c_size_t, _vp,
+                           ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+        "crs_state_eval_conc": [_vp, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp,
+                                _vp],
+        "crs_state_eval_rxn_rates": [_vp, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp],
+        "crs_state_get_rxn_pres_mod": [_vp, ctypes.c_double, ctypes.c_double, _vp, _vp],
+        "crs_state_eval_spec_rates": [_vp, _vp, _vp, _vp, _vp, _vp],
+        "crs_state_eval_thermo": [_vp, _i32, ctypes.c_double, _vp],
+        "crs_state_eval_conc_rho": [_vp, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp,
+                                    _vp, _vp],
+        "crs_state_dydt": [_vp, _i32, ctypes.c_double, _vp, _vp],
         "crs_wdot_gemm_noalloc": [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp],
         "crs_gemm_bf16": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp],
         "crs_mlp_forward": [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _i32, _vp, _i64,

@@ -3,7 +3,8 @@
     python -m create_rate_subs_gb300.build [--force]
 
 Each .cu file in csrc/ is compiled in parallel for sm_103a only
-(``-gencode arch=compute_103a,code=sm_103a``), then linked into
+(``-gencode arch=compute_103a,code=sm_103a``), each .cpp file (host-only
+code) by the host C++ compiler, then everything is linked into
 create_rate_subs_gb300/lib/libcrs.so with the CUDA runtime linked
 statically, so that loading it needs nothing beyond the driver.
 """
@@ -30,6 +31,11 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 EXTRA = {"crs_fp64_strict.cu": ["-fmad=false"],
          # thermo utilities in the emitted operand order, bit for bit
          "crs_dydt.cu": ["-fmad=false"]}
+# Host-only sources: the reentrant per-state functions, which must round
+# every operation as the reference's emitted C does (no contraction into
+# FMA, no fast math), whatever the host architecture's default.
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+              "-I", os.path.join(REPO, "include")]
 
 
 def nvcc():
@@ -43,7 +49,15 @@ def nvcc():
 
 
 def sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def cxx():
+    for name in ("g++", "c++"):
+        p = shutil.which(name)
+        if p:
+            return p
+    raise RuntimeError("no host C++ compiler (g++) found")
 
 
 def _stale(force):
@@ -66,9 +80,12 @@ def build(force=False, verbose=False):
     cc = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = ([cc] + ARCH + COMMON + EXTRA.get(src, [])
-               + ["-c", os.path.join(CSRC, src), "-o", obj])
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        if src.endswith(".cpp"):
+            cmd = [cxx()] + HOST_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        else:
+            cmd = ([cc] + ARCH + COMMON + EXTRA.get(src, [])
+                   + ["-c", os.path.join(CSRC, src), "-o", obj])
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, res.stdout, res.stderr))

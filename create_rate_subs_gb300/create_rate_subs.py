@@ -9,16 +9,22 @@ output in ``./out/``.  Differences, all deliberate:
 * ``-ls`` is honoured (the reference parses it and then drops it,
   create_rate_subs.py:593);
 * instead of unrolled source, every target writes the mechanism tables
-  (``out/mech.crs``, loaded by ``crs_mech_load_file``) and headers that
-  declare the reference's four per-state functions, implemented by libcrs:
-  ``c`` -> header.h, chem_utils.h, rates.h; ``cuda`` -> the same with .cuh
-  names; ``gb300`` -> both sets;
+  (``out/mech.crs``, loaded by ``crs_mech_load_file``) and headers for the
+  reference's per-state functions:
+  ``c`` -> header.h, chem_utils.h, rates.h, dydt.h: host declarations,
+  implemented by libcrs (crs.h; bind the loaded tables with crs_bind);
+  ``cuda`` -> header.cuh, chem_utils.cuh, rates.cuh, dydt.cuh: __device__
+  definitions (include/crs_device.cuh) over the mechanism's table image,
+  written as mech_image.cuh, with the headers they include copied beside
+  them, so that a user's kernel calls them per thread as it calls the
+  reference's emitted CUDA; ``gb300`` -> both sets;
 * ``fortran`` and ``matlab`` are refused (the reference itself marks them
   incomplete, create_rate_subs.py:459-460).
 """
 
 import argparse
 import os
+import shutil
 import sys
 
 from .mech_interpret import MechanismError
@@ -37,8 +43,9 @@ def _header(mech):
     lines += [" */", "#define NSP %d" % mech.n_species,
               "/** Number of variables. NN = NSP + 1 (temperature). */",
               "#define NN %d" % (mech.n_species + 1),
+              "/** Reactions, reversible reactions, pres_mod entries. */",
               "#define NRXN %d" % mech.n_reactions,
-              "#define NREV %d" % mech.n_rev,
+              "#define NRXN_REV %d" % mech.n_rev,
               "#define NPDEP %d" % mech.n_pdep, "", "#endif", ""]
     return "\n".join(lines)
 
@@ -56,10 +63,72 @@ def _decls(kind):
                 "double*);\n")
     guard = "CRS_%s_HEAD" % kind.upper()
     return ("#ifndef %s\n#define %s\n\n#include \"header.h\"\n\n"
-            "/* Implemented by libcrs (include/crs.h) on the GPU.  Load out/mech.crs\n"
-            " * with crs_mech_load_file and select it with crs_bind first. */\n"
+            "/* Implemented by libcrs (include/crs.h) on the host, reentrant.  Load\n"
+            " * out/mech.crs with crs_mech_load_file or crs_mech_load_host and select\n"
+            " * it with crs_bind (or crs_bind_thread) first. */\n"
             "#ifdef __cplusplus\nextern \"C\" {\n#endif\n%s"
             "#ifdef __cplusplus\n}\n#endif\n\n#endif\n" % (guard, guard, body))
+
+
+def _dydt_decls():
+    return ("#ifndef CRS_DYDT_HEAD\n#define CRS_DYDT_HEAD\n\n#include \"header.h\"\n\n"
+            "/* Implemented by libcrs (include/crs.h) on the host: constant pressure\n"
+            " * unless crs_dydt_form(1) selects constant volume. */\n"
+            "#ifdef __cplusplus\nextern \"C\" {\n#endif\n"
+            "void dydt (const double, const double, const double*, double*);\n"
+            "#ifdef __cplusplus\n}\n#endif\n\n#endif\n")
+
+
+def table_image(blob):
+    """(image bytes, layout int32 words) of a mechanism blob, built by
+    libcrs on the host (crs_mech_image)."""
+    import ctypes
+    from . import _lib
+    lib = _lib.load()
+    sizes = (ctypes.c_size_t * 2)()
+    _lib.check(lib.crs_mech_image(blob, len(blob), None, 0, None, 0, sizes))
+    img = ctypes.create_string_buffer(int(sizes[0]))
+    lay = (ctypes.c_int32 * int(sizes[1]))()
+    _lib.check(lib.crs_mech_image(blob, len(blob), img, sizes[0], lay, sizes[1], sizes))
+    return img.raw[: int(sizes[0])], list(lay)
+
+
+def _image_header(mech):
+    """mech_image.cuh: the table image as a __device__ array and its
+    layout as a __constant__ crs::ImgLayout (crs_tables.h), for
+    crs_device.cuh."""
+    img, lay = table_image(mech.blob)
+    if len(img) % 8:
+        img = img + b"\0" * (8 - len(img) % 8)
+    words = [int.from_bytes(img[i:i + 8], "little") for i in range(0, len(img), 8)]
+    out = ["/* Table image of the mechanism (%d species, %d reactions) for the per-state"
+           % (mech.n_species, mech.n_reactions),
+           " * device functions of crs_device.cuh; written by create_rate_subs_gb300. */",
+           "#ifndef CRS_MECH_IMAGE_CUH", "#define CRS_MECH_IMAGE_CUH", "",
+           "#include \"crs_tables.h\"", "",
+           "#define CRS_MECH_IMAGE_DEFINED 1",
+           "#define CRS_MECH_NSP %d" % mech.n_species,
+           "#define CRS_MECH_NRXN %d" % mech.n_reactions,
+           "#define CRS_MECH_NREV %d" % mech.n_rev,
+           "#define CRS_MECH_NPDEP %d" % mech.n_pdep, "",
+           "static __device__ __align__(16) const unsigned long long crs_mech_image_words[%d] = {"
+           % len(words)]
+    for i in range(0, len(words), 6):
+        out.append("  " + ", ".join("0x%016xull" % w for w in words[i:i + 6]) + ",")
+    out.append("};")
+    out.append("#define crs_mech_image "
+               "(reinterpret_cast<const unsigned char *>(crs_mech_image_words))")
+    out.append("static __constant__ crs::ImgLayout crs_mech_layout = {")
+    for i in range(0, len(lay), 12):
+        out.append("  " + ", ".join(str(v) for v in lay[i:i + 12]) + ",")
+    out += ["};", "", "#endif", ""]
+    return "\n".join(out)
+
+
+def _device_header(guard):
+    return ("#ifndef %s\n#define %s\n\n#include \"header.cuh\"\n"
+            "#include \"mech_image.cuh\"\n#include \"crs_device.cuh\"\n\n#endif\n"
+            % (guard, guard))
 
 
 def create_rate_subs(lang, mech_name, therm_name=None, last_spec=None,
@@ -78,14 +147,24 @@ def create_rate_subs(lang, mech_name, therm_name=None, last_spec=None,
     create_dir(out_dir)
     with open(os.path.join(out_dir, "mech.crs"), "wb") as f:
         f.write(mech.blob)
-    exts = {"c": [".h"], "cuda": [".cuh"], "gb300": [".h", ".cuh"]}[lang]
-    for ext in exts:
-        with open(os.path.join(out_dir, "header" + ext), "w") as f:
-            f.write(_header(mech))
-        with open(os.path.join(out_dir, "chem_utils" + ext), "w") as f:
-            f.write(_decls("chem_utils").replace('"header.h"', '"header%s"' % ext))
-        with open(os.path.join(out_dir, "rates" + ext), "w") as f:
-            f.write(_decls("rates").replace('"header.h"', '"header%s"' % ext))
+    if lang in ("c", "gb300"):
+        files = {"header.h": _header(mech), "chem_utils.h": _decls("chem_utils"),
+                 "rates.h": _decls("rates"), "dydt.h": _dydt_decls()}
+        for name, text in files.items():
+            with open(os.path.join(out_dir, name), "w") as f:
+                f.write(text)
+    if lang in ("cuda", "gb300"):
+        files = {"header.cuh": _header(mech), "mech_image.cuh": _image_header(mech),
+                 "chem_utils.cuh": _device_header("CRS_CHEM_UTILS_CUH"),
+                 "rates.cuh": _device_header("CRS_RATES_CUH"),
+                 "dydt.cuh": _device_header("CRS_DYDT_CUH")}
+        for name, text in files.items():
+            with open(os.path.join(out_dir, name), "w") as f:
+                f.write(text)
+        inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "include")
+        for name in ("crs_tables.h", "crs_eval.h", "crs_device.cuh"):
+            shutil.copy(os.path.join(inc, name), os.path.join(out_dir, name))
     return mech
 
 
@@ -94,8 +173,9 @@ def main(argv=None):
         description="Generates mechanism tables for the GB300 species and "
                     "reaction rate library.")
     ap.add_argument("-l", "--lang", type=str, choices=langs, required=True,
-                    help="Target: c, cuda (headers for the reference's "
-                         "function names) or gb300 (both).")
+                    help="Target: c (host declarations, implemented by "
+                         "libcrs), cuda (device definitions over the "
+                         "mechanism's table image) or gb300 (both).")
     ap.add_argument("-i", "--input", type=str, required=True,
                     help="Input mechanism filename (e.g., mech.dat).")
     ap.add_argument("-t", "--thermo", type=str, default=None,

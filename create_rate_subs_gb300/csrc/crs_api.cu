@@ -46,6 +46,20 @@ cudaError_t launch_gemm_wdot(const void *A, const void *B, int64_t M_pad, int64_
 // Tables the fast kernels derive from the blob's tables at load time.
 bool build_fast_tables(const std::vector<unsigned char> &img,
                        const ImgLayout &L, std::vector<Derived> &extra);
+// Reentrant per-state evaluation on the host (crs_host.cpp).
+namespace host {
+void eval_conc(const Tab &t, double T, double pres, const double *y, double *y_N,
+               double *mw_avg, double *rho, double *conc);
+void eval_rxn_rates(const Tab &t, double T, double pres, const double *C, double *fwd,
+                    double *rev);
+void get_rxn_pres_mod(const Tab &t, double T, double pres, const double *C, double *pm);
+void eval_spec_rates(const Tab &t, const double *fwd, const double *rev, const double *pm,
+                     double *sp_rates, double *dy_N);
+void eval_thermo(const Tab &t, int which, double T, double *out);
+void eval_conc_rho(const Tab &t, double T, double rho, const double *y, double *y_N,
+                   double *mw_avg, double *pres, double *conc);
+void dydt(const Tab &t, int conv, double p_or_rho, const double *y, double *dy);
+}  // namespace host
 }  // namespace crs
 
 // Dynamic-scheduling slots per mechanism handle: the most launches of the
@@ -65,6 +79,7 @@ struct crs_mech {
   unsigned long long *d_sched = nullptr;
   mutable std::atomic<unsigned> sched_next{0};
   std::vector<unsigned char> h_img;
+  crs::Tab htab{};  // view of h_img for the per-state host functions
   // tensor-core contraction (CRS_MODE_GEMM): nu as a bf16 matrix
   // [N_pad][2*Kh] (each row nu_k, then nu_k again for the lo half), and a
   // workspace for one chunk of states (bf16 rows + per-state exponents),
@@ -83,6 +98,8 @@ struct crs_mech {
   double *d_host = nullptr;
   int64_t host_chunk = 0;
 };
+
+void unbind(const crs_mech *m);
 
 namespace {
 
@@ -418,6 +435,8 @@ bool check_device(const crs_mech *m) {
 
 int check_batch(const crs_mech *m, int64_t n, int64_t ld) {
   if (!m) return fail(CRS_ERR_ARG, "mechanism is NULL");
+  if (!m->d_img)
+    return fail(CRS_ERR_ARG, "mechanism has no device tables (loaded with crs_mech_load_host)");
   if (n < 0) return fail(CRS_ERR_ARG, "n < 0");
   if (ld < n) return fail(CRS_ERR_ARG, "ld < n");
   if (!check_device(m)) return CRS_ERR_ARG;
@@ -570,6 +589,7 @@ int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
     delete m;
     return rc;
   }
+  m->htab = crs::make_tab(m->h_img.data(), m->L);
   cudaError_t e = cudaGetDevice(&m->device);
   if (e == cudaSuccess)
     e = cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
@@ -593,6 +613,41 @@ int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
   // 128-byte alignment of the dynamic part pads to 128 bytes) and slack
   m->smem_optin -= 256;
   *out = m;
+  return CRS_OK;
+}
+
+int crs_mech_load_host(const void *blob, size_t nbytes, crs_mech **out) {
+  if (!blob || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  crs_mech *m = new crs_mech();
+  int rc = build_image(static_cast<const unsigned char *>(blob), nbytes, m);
+  if (rc != CRS_OK) {
+    delete m;
+    return rc;
+  }
+  m->device = -1;
+  m->htab = crs::make_tab(m->h_img.data(), m->L);
+  *out = m;
+  return CRS_OK;
+}
+
+int crs_mech_image(const void *blob, size_t nbytes, void *img, size_t img_cap,
+                   int32_t *layout, size_t layout_cap, size_t sizes[2]) {
+  if (!blob || !sizes) return fail(CRS_ERR_ARG, "NULL argument");
+  crs_mech m;
+  int rc = build_image(static_cast<const unsigned char *>(blob), nbytes, &m);
+  if (rc != CRS_OK) return rc;
+  static_assert(sizeof(crs::ImgLayout) % sizeof(int32_t) == 0, "layout of int32 words");
+  sizes[0] = m.h_img.size();
+  sizes[1] = sizeof(crs::ImgLayout) / sizeof(int32_t);
+  if (img) {
+    if (img_cap < sizes[0]) return fail(CRS_ERR_ARG, "image buffer too small");
+    memcpy(img, m.h_img.data(), sizes[0]);
+  }
+  if (layout) {
+    if (layout_cap < sizes[1]) return fail(CRS_ERR_ARG, "layout buffer too small");
+    memcpy(layout, &m.L, sizeof(crs::ImgLayout));
+  }
   return CRS_OK;
 }
 
@@ -626,6 +681,7 @@ int crs_mech_load_file(const char *path, crs_mech **out) {
 
 int crs_mech_free(crs_mech *m) {
   if (!m) return CRS_OK;
+  unbind(m);
   if (m->d_img) cudaFree(m->d_img);
   if (m->d_status) cudaFree(m->d_status);
   if (m->d_sched) cudaFree(m->d_sched);
@@ -651,6 +707,7 @@ int crs_mech_dims(const crs_mech *m, int64_t out[5]) {
 
 int crs_status(const crs_mech *m, void *stream, int32_t out[2]) {
   if (!m || !out) return fail(CRS_ERR_ARG, "NULL argument");
+  if (!m->d_status) return fail(CRS_ERR_ARG, "mechanism has no device tables");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(out, m->d_status, 2 * sizeof(int32_t),
                                   cudaMemcpyDeviceToHost, s);
@@ -660,6 +717,7 @@ int crs_status(const crs_mech *m, void *stream, int32_t out[2]) {
 
 int crs_status_reset(const crs_mech *m, void *stream) {
   if (!m) return fail(CRS_ERR_ARG, "NULL argument");
+  if (!m->d_status) return fail(CRS_ERR_ARG, "mechanism has no device tables");
   cudaError_t e = cudaMemsetAsync(m->d_status, 0, 2 * sizeof(int32_t),
                                   static_cast<cudaStream_t>(stream));
   return e == cudaSuccess ? CRS_OK : cuda_fail(e, "crs_status_reset");
@@ -866,240 +924,172 @@ int crs_wdot_host(const crs_mech *m, int64_t n, const double *T, const double *P
 }  // extern "C"
 
 // ---- per-state drop-in ---------------------------------------------------
-namespace {
-struct Bound {
-  std::mutex mu;
-  const crs_mech *m = nullptr;
-  double *d = nullptr;  // device scratch for one state
-  size_t words = 0;
-};
-Bound g_bound;
+//
+// The reference's per-state functions are pure host functions with the
+// mechanism baked in.  Here they evaluate the bound mechanism's host table
+// image on the calling thread (crs_host.cpp): no lock, no device, no
+// allocation, safe from any number of threads at once.
 
-void fill_nan(double *p, int n) {
-  if (!p) return;
-  for (int i = 0; i < n; ++i) p[i] = __builtin_nan("");
+extern "C" {
+
+#define CRS_STATE_CHECK(m, name)                                        \
+  do {                                                                  \
+    if (!(m)) return fail(CRS_ERR_ARG, "%s: mechanism is NULL", name);  \
+  } while (0)
+
+int crs_state_eval_conc(const crs_mech *m, double T, double pres, const double *y,
+                        double *y_N, double *mw_avg, double *rho, double *conc) {
+  CRS_STATE_CHECK(m, "crs_state_eval_conc");
+  if ((!y && m->L.N > 1) || !y_N || !mw_avg || !rho || !conc)
+    return fail(CRS_ERR_ARG, "crs_state_eval_conc: NULL array");
+  crs::host::eval_conc(m->htab, T, pres, y, y_N, mw_avg, rho, conc);
+  return CRS_OK;
 }
 
-// Device scratch for one state: T, P, y/C [N], fwd [R], rev [R_rev],
-// pm [N_pm], wdot [N], y_N, mw, rho.
-struct One {
-  double *T, *P, *C, *fwd, *rev, *pm, *w, *misc;
-};
-One layout(const crs_mech *m, double *d) {
-  One o;
-  const crs::ImgLayout &L = m->L;
-  o.T = d;
-  o.P = d + 1;
-  o.C = d + 2;
-  o.fwd = o.C + L.N;
-  o.rev = o.fwd + L.R;
-  o.pm = o.rev + (L.NREV > 0 ? L.NREV : 1);
-  o.w = o.pm + (L.NPM > 0 ? L.NPM : 1);
-  o.misc = o.w + L.N;
-  return o;
+int crs_state_eval_rxn_rates(const crs_mech *m, double T, double pres, const double *C,
+                             double *fwd, double *rev) {
+  CRS_STATE_CHECK(m, "crs_state_eval_rxn_rates");
+  if (!C || (!fwd && m->L.R > 0) || (!rev && m->L.NREV > 0))
+    return fail(CRS_ERR_ARG, "crs_state_eval_rxn_rates: NULL array");
+  crs::host::eval_rxn_rates(m->htab, T, pres, C, fwd, rev);
+  return CRS_OK;
+}
+
+int crs_state_get_rxn_pres_mod(const crs_mech *m, double T, double pres, const double *C,
+                               double *pres_mod) {
+  CRS_STATE_CHECK(m, "crs_state_get_rxn_pres_mod");
+  if (!C || (!pres_mod && m->L.NPM > 0))
+    return fail(CRS_ERR_ARG, "crs_state_get_rxn_pres_mod: NULL array");
+  crs::host::get_rxn_pres_mod(m->htab, T, pres, C, pres_mod);
+  return CRS_OK;
+}
+
+int crs_state_eval_spec_rates(const crs_mech *m, const double *fwd, const double *rev,
+                              const double *pres_mod, double *sp_rates, double *dy_N) {
+  CRS_STATE_CHECK(m, "crs_state_eval_spec_rates");
+  if ((!fwd && m->L.R > 0) || (!rev && m->L.NREV > 0) || (!pres_mod && m->L.NPM > 0) ||
+      (!sp_rates && m->L.N > 1) || !dy_N)
+    return fail(CRS_ERR_ARG, "crs_state_eval_spec_rates: NULL array");
+  crs::host::eval_spec_rates(m->htab, fwd, rev, pres_mod, sp_rates, dy_N);
+  return CRS_OK;
+}
+
+int crs_state_eval_thermo(const crs_mech *m, int which, double T, double *out) {
+  CRS_STATE_CHECK(m, "crs_state_eval_thermo");
+  if (which < 0 || which > 3) return fail(CRS_ERR_ARG, "which must be 0..3 (h, u, cv, cp)");
+  if (!out) return fail(CRS_ERR_ARG, "crs_state_eval_thermo: NULL array");
+  crs::host::eval_thermo(m->htab, which, T, out);
+  return CRS_OK;
+}
+
+int crs_state_eval_conc_rho(const crs_mech *m, double T, double rho, const double *y,
+                            double *y_N, double *mw_avg, double *pres, double *conc) {
+  CRS_STATE_CHECK(m, "crs_state_eval_conc_rho");
+  if ((!y && m->L.N > 1) || !y_N || !mw_avg || !pres || !conc)
+    return fail(CRS_ERR_ARG, "crs_state_eval_conc_rho: NULL array");
+  crs::host::eval_conc_rho(m->htab, T, rho, y, y_N, mw_avg, pres, conc);
+  return CRS_OK;
+}
+
+int crs_state_dydt(const crs_mech *m, int conv, double p_or_rho, const double *y, double *dy) {
+  CRS_STATE_CHECK(m, "crs_state_dydt");
+  if (conv != 0 && conv != 1) return fail(CRS_ERR_ARG, "conv must be 0 or 1");
+  if (!y || !dy) return fail(CRS_ERR_ARG, "crs_state_dydt: NULL array");
+  crs::host::dydt(m->htab, conv, p_or_rho, y, dy);
+  return CRS_OK;
+}
+
+#undef CRS_STATE_CHECK
+
+}  // extern "C"
+
+namespace {
+// The mechanism of the reference-signature functions: the calling thread's
+// own binding (crs_bind_thread) if it has one, else the process-wide one
+// (crs_bind).  Reads are lock-free; a handle is immutable after load.
+std::atomic<const crs_mech *> g_bound{nullptr};
+thread_local const crs_mech *t_bound = nullptr;
+std::atomic<int> g_dydt_conv{0};  // form of the per-state dydt (crs_dydt_form)
+
+const crs_mech *bound(const char *name) {
+  const crs_mech *m = t_bound ? t_bound : g_bound.load(std::memory_order_acquire);
+  if (!m) fail(CRS_ERR_NOMECH, "%s: no mechanism bound (crs_bind / crs_bind_thread)", name);
+  return m;
 }
 }  // namespace
+
+// Called by crs_mech_free: a freed handle stays bound nowhere that this
+// thread or the process-wide binding can reach.
+void unbind(const crs_mech *m) {
+  const crs_mech *expected = m;
+  g_bound.compare_exchange_strong(expected, nullptr);
+  if (t_bound == m) t_bound = nullptr;
+}
 
 extern "C" {
 
 int crs_bind(const crs_mech *m) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  if (g_bound.d) {
-    cudaFree(g_bound.d);
-    g_bound.d = nullptr;
-  }
-  g_bound.m = m;
-  if (!m) return CRS_OK;
-  const crs::ImgLayout &L = m->L;
-  g_bound.words = 2 + 2 * (size_t)L.N + L.R + (L.NREV + 1) + (L.NPM + 1) + 3;
-  cudaError_t e = cudaMalloc(&g_bound.d, g_bound.words * sizeof(double));
-  if (e != cudaSuccess) {
-    g_bound.m = nullptr;
-    return cuda_fail(e, "crs_bind");
-  }
+  g_bound.store(m, std::memory_order_release);
   return CRS_OK;
 }
 
+int crs_bind_thread(const crs_mech *m) {
+  t_bound = m;
+  return CRS_OK;
+}
+
+// rate_subs.py:1297-1299 (chem_utils.h)
 void eval_conc(const double T, const double pres, const double *y, double *y_N,
                double *mw_avg, double *rho, double *conc) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "eval_conc: no mechanism bound (crs_bind)");
-    return;
-  }
-  One o = layout(m, g_bound.d);
-  const int N = m->L.N;
-  double tp[2] = {T, pres};
-  crs::Batch b = make_batch(m, 1, 1);
-  b.T = o.T; b.P = o.P; b.Y = o.C; b.conc = o.w;
-  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(o.C, y, (N - 1) * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = crs::launch_stage(0, m->d_img, m->L, b, o.misc, o.misc + 1, o.misc + 2,
-                          m->sm_count, 0);
-  double misc[3];
-  if (e == cudaSuccess)
-    e = cudaMemcpy(conc, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(misc, o.misc, sizeof misc, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, "eval_conc");
-    fill_nan(conc, N);
-    misc[0] = misc[1] = misc[2] = __builtin_nan("");
-  }
-  *y_N = misc[0];
-  *mw_avg = misc[1];
-  *rho = misc[2];
+  if (const crs_mech *m = bound("eval_conc"))
+    crs::host::eval_conc(m->htab, T, pres, y, y_N, mw_avg, rho, conc);
 }
 
+// rate_subs.py:287-290 (rates.h)
 void eval_rxn_rates(const double T, const double pres, const double *C,
                     double *fwd_rxn_rates, double *rev_rxn_rates) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "eval_rxn_rates: no mechanism bound (crs_bind)");
-    return;
-  }
-  One o = layout(m, g_bound.d);
-  const crs::ImgLayout &L = m->L;
-  double tp[2] = {T, pres};
-  crs::Batch b = make_batch(m, 1, 1);
-  b.T = o.T; b.P = o.P; b.conc = o.C; b.fwd = o.fwd; b.rev = o.rev;
-  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(o.C, C, L.N * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = crs::launch_stage(1, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(fwd_rxn_rates, o.fwd, L.R * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && L.NREV > 0)
-    e = cudaMemcpy(rev_rxn_rates, o.rev, L.NREV * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, "eval_rxn_rates");
-    fill_nan(fwd_rxn_rates, L.R);
-    fill_nan(rev_rxn_rates, L.NREV);
-  }
+  if (const crs_mech *m = bound("eval_rxn_rates"))
+    crs::host::eval_rxn_rates(m->htab, T, pres, C, fwd_rxn_rates, rev_rxn_rates);
 }
 
+// rate_subs.py:761-763 (rates.h)
 void get_rxn_pres_mod(const double T, const double pres, const double *C,
                       double *pres_mod) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "get_rxn_pres_mod: no mechanism bound (crs_bind)");
-    return;
-  }
-  const crs::ImgLayout &L = m->L;
-  if (L.NPM == 0) return;
-  One o = layout(m, g_bound.d);
-  double tp[2] = {T, pres};
-  crs::Batch b = make_batch(m, 1, 1);
-  b.T = o.T; b.P = o.P; b.conc = o.C; b.pm = o.pm;
-  cudaError_t e = cudaMemcpy(o.T, tp, sizeof tp, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(o.C, C, L.N * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = crs::launch_stage(2, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(pres_mod, o.pm, L.NPM * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, "get_rxn_pres_mod");
-    fill_nan(pres_mod, L.NPM);
-  }
+  if (const crs_mech *m = bound("get_rxn_pres_mod"))
+    crs::host::get_rxn_pres_mod(m->htab, T, pres, C, pres_mod);
 }
 
+// rate_subs.py:1124-1127 (rates.h)
 void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
                      const double *pres_mod, double *sp_rates, double *dy_N) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "eval_spec_rates: no mechanism bound (crs_bind)");
-    return;
-  }
-  const crs::ImgLayout &L = m->L;
-  One o = layout(m, g_bound.d);
-  crs::Batch b = make_batch(m, 1, 1);
-  b.fwd = o.fwd; b.rev = o.rev; b.pm = o.pm; b.wdot = o.w;
-  cudaError_t e = cudaMemcpy(o.fwd, fwd_rates, L.R * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && L.NREV > 0)
-    e = cudaMemcpy(o.rev, rev_rates, L.NREV * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && L.NPM > 0)
-    e = cudaMemcpy(o.pm, pres_mod, L.NPM * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = crs::launch_stage(3, m->d_img, L, b, nullptr, nullptr, nullptr, m->sm_count, 0);
-  std::vector<double> w(L.N);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(w.data(), o.w, L.N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, "eval_spec_rates");
-    fill_nan(w.data(), L.N);
-  }
-  for (int k = 0; k < L.N - 1; ++k) sp_rates[k] = w[k];
-  *dy_N = w[L.N - 1];
+  if (const crs_mech *m = bound("eval_spec_rates"))
+    crs::host::eval_spec_rates(m->htab, fwd_rates, rev_rates, pres_mod, sp_rates, dy_N);
 }
-
-namespace {
-int g_dydt_conv = 0;  // form of the per-state dydt (crs_dydt_form)
-
-void thermo_one(int which, const char *name, double T, double *out) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "%s: no mechanism bound (crs_bind)", name);
-    return;
-  }
-  One o = layout(m, g_bound.d);
-  const int N = m->L.N;
-  cudaError_t e = cudaMemcpy(o.T, &T, sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = crs::launch_thermo(m->d_img, m->L, which, 1, o.T, 1, o.w, m->sm_count, 0);
-  if (e == cudaSuccess) e = cudaMemcpy(out, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, name);
-    fill_nan(out, N);
-  }
-}
-}  // namespace
 
 // rate_subs.py:1497-1776 (chem_utils.h :1276-1279)
-void eval_h(const double T, double *h) { thermo_one(0, "eval_h", T, h); }
-void eval_u(const double T, double *u) { thermo_one(1, "eval_u", T, u); }
-void eval_cv(const double T, double *cv) { thermo_one(2, "eval_cv", T, cv); }
-void eval_cp(const double T, double *cp) { thermo_one(3, "eval_cp", T, cp); }
+void eval_h(const double T, double *h) {
+  if (const crs_mech *m = bound("eval_h")) crs::host::eval_thermo(m->htab, 0, T, h);
+}
+void eval_u(const double T, double *u) {
+  if (const crs_mech *m = bound("eval_u")) crs::host::eval_thermo(m->htab, 1, T, u);
+}
+void eval_cv(const double T, double *cv) {
+  if (const crs_mech *m = bound("eval_cv")) crs::host::eval_thermo(m->htab, 2, T, cv);
+}
+void eval_cp(const double T, double *cp) {
+  if (const crs_mech *m = bound("eval_cp")) crs::host::eval_thermo(m->htab, 3, T, cp);
+}
 
 // rate_subs.py:1396-1490 (chem_utils.h :1274-1275)
 void eval_conc_rho(const double T, const double rho, const double *y, double *y_N,
                    double *mw_avg, double *pres, double *conc) {
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "eval_conc_rho: no mechanism bound (crs_bind)");
-    return;
-  }
-  One o = layout(m, g_bound.d);
-  const int N = m->L.N;
-  double tr[2] = {T, rho};
-  cudaError_t e = cudaMemcpy(o.T, tr, sizeof tr, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && N > 1)
-    e = cudaMemcpy(o.C, y, (N - 1) * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = crs::launch_conc_rho(m->d_img, m->L, 1, o.T, o.P, o.C, 1, o.misc, o.misc + 1,
-                             o.misc + 2, o.w, m->sm_count, 0);
-  double misc[3];
-  if (e == cudaSuccess) e = cudaMemcpy(conc, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(misc, o.misc, sizeof misc, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    cuda_fail(e, "eval_conc_rho");
-    fill_nan(conc, N);
-    misc[0] = misc[1] = misc[2] = __builtin_nan("");
-  }
-  *y_N = misc[0];
-  *mw_avg = misc[1];
-  *pres = misc[2];
+  if (const crs_mech *m = bound("eval_conc_rho"))
+    crs::host::eval_conc_rho(m->htab, T, rho, y, y_N, mw_avg, pres, conc);
 }
 
 int crs_dydt_form(int conv) {
   if (conv != 0 && conv != 1) return fail(CRS_ERR_ARG, "conv must be 0 or 1");
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  g_dydt_conv = conv;
+  g_dydt_conv.store(conv);
   return CRS_OK;
 }
 
@@ -1108,24 +1098,8 @@ int crs_dydt_form(int conv) {
 // volume, after crs_dydt_form(1)), as the emitted CONP / CONV builds read it.
 void dydt(const double t, const double pres, const double *y, double *dy) {
   (void)t;
-  std::lock_guard<std::mutex> lk(g_bound.mu);
-  const crs_mech *m = g_bound.m;
-  if (!m) {
-    fail(CRS_ERR_NOMECH, "dydt: no mechanism bound (crs_bind)");
-    return;
-  }
-  One o = layout(m, g_bound.d);
-  const int N = m->L.N;
-  cudaError_t e = cudaMemcpy(o.P, &pres, sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(o.C, y, N * sizeof(double), cudaMemcpyHostToDevice);
-  int rc = e == cudaSuccess ? CRS_OK : cuda_fail(e, "dydt");
-  if (rc == CRS_OK)
-    rc = crs_dydt(m, 1, o.P, o.C, 1, o.w, g_dydt_conv, CRS_MODE_FP64_STRICT, nullptr);
-  if (rc == CRS_OK) {
-    e = cudaMemcpy(dy, o.w, N * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) rc = cuda_fail(e, "dydt");
-  }
-  if (rc != CRS_OK) fill_nan(dy, N);
+  if (const crs_mech *m = bound("dydt"))
+    crs::host::dydt(m->htab, g_dydt_conv.load(), pres, y, dy);
 }
 
 }  // extern "C"

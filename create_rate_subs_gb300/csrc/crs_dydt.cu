@@ -21,22 +21,11 @@
 namespace crs {
 namespace thermo {
 
-constexpr double RU_PRINTED = 8.31446210e+03;  // RU as eval_conc prints it (%.8e)
+using ref::RU_PRINTED;  // RU as eval_conc prints it (%.8e)
 
-// h (which 0), u (1), cv (2), cp (3) of species k at T, J/kg or J/(kg K)
+// h (which 0), u (1), cv (2), cp (3) of species k at T (include/crs_eval.h)
 __device__ __forceinline__ double value(const double *c, int which, double T) {
-  const double *a = c + ((T <= c[2]) ? 4 : 14);
-  const double rm = c[0];
-  switch (which) {
-    case 0:
-      return rm * (a[5] + T * (a[0] + T * (a[6] + T * (a[7] + T * (a[8] + a[9] * T)))));
-    case 1:
-      return rm * (a[5] + T * (a[0] - 1.0 + T * (a[6] + T * (a[7] + T * (a[8] + a[9] * T)))));
-    case 2:
-      return rm * (a[0] - 1.0 + T * (a[1] + T * (a[2] + T * (a[3] + a[4] * T))));
-    default:
-      return rm * (a[0] + T * (a[1] + T * (a[2] + T * (a[3] + a[4] * T))));
-  }
+  return ref::thermo_value(c, which, T);
 }
 
 __global__ void k_thermo(const unsigned char *__restrict__ img, ImgLayout L, int which,

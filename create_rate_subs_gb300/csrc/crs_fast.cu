@@ -763,15 +763,19 @@ __global__ void __launch_bounds__(DW * 32)
       const double P = bP[j];
       s.P = P;
       // concentrations (lanes over species)
-      double ys = 0.0, mw = 0.0;
+      double mw = 0.0;
       for (int k = lane; k < N - 1; k += 32) {
         const double y = b.Y[(int64_t)k * b.ld + i];
         C[k] = y;
-        ys += y;
         mw = fma(y, t.inv_mw[k], mw);
       }
-      ys = warp_sum(ys);
       mw = warp_sum(mw);
+      __syncwarp();
+      // y_N = 1 - sum y in the reference's left-to-right order on every
+      // lane (rate_subs.py:1312-1320): where the bath gas is scarce, the
+      // rounding of this difference is a large relative error of C_N
+      double ys = N > 1 ? C[0] : 0.0;
+      for (int k = 1; k < N - 1; ++k) ys += C[k];
       const double yN = 1.0 - ys;
       mw = fma(yN, t.inv_mw[N - 1], mw);
       const double rho = P / mw * (s.invT * INV_RU);

@@ -1,153 +1,21 @@
-// Internal layout shared by the libcrs kernels and the host ABI.
+// Internal declarations shared by the libcrs kernels and the host ABI.
 //
-// A mechanism lives on the device as one contiguous "table image": every
-// table of create_rate_subs_gb300/tables.py, each section 16-byte aligned,
-// so that one CTA can stage the whole image into shared memory with
-// cp.async.bulk.  ImgLayout carries the byte offsets (it is passed by value
-// as a kernel parameter).
+// The table image (include/crs_tables.h) is staged whole or in ranges into
+// shared memory with cp.async.bulk, each section 16-byte aligned;
+// ImgLayout is passed by value as a kernel parameter.
 #pragma once
 
 #include <cstdint>
 #include <vector>
 #include <cuda_runtime.h>
 
-namespace crs {
+#include "../../include/crs_eval.h"
+#include "../../include/crs_tables.h"
 
-enum { RATE_CONST = 0, RATE_EXP = 1, RATE_NEGEXP = 2, RATE_POW = 3, RATE_PLOG = 4,
-       RATE_CHEB = 5 };
-constexpr int CHEB_MAX = 16;  // most Chebyshev temperature terms (checked at load)
-enum { PM_THD = 0, PM_FALL_LOW = 1, PM_FALL_HIGH = 2 };
-enum { FORM_LINDEMANN = 0, FORM_TROE = 1, FORM_SRI = 2 };
+namespace crs {
 
 // Status word bits (device, one per mechanism handle).
 enum { STATUS_STAGE_TIMEOUT = 1, STATUS_GEMM_TIMEOUT = 2 };
-
-struct ImgLayout {
-  int N, R, NREV, NPM, NRATE, NKC;
-  int bytes;  // image size, multiple of 16
-  // Byte ranges [lo, hi) of the image that each fast kernel stages into
-  // shared memory (two ranges per kernel, copied back to back); sections
-  // outside them are read from global memory through L1.
-  //   [0] FP64 one state per thread   [1] FP64 one state per warp
-  //   [2] mixed one state per thread, Kc polynomials read through L1
-  //   [3] mixed one state per warp
-  //   [4] mixed one state per thread, Kc polynomials in shared memory
-  int rng[5][4];
-  // derived f64 sections (fast kernels): per rate row (logA, b, -Ta); per
-  // reversible reaction log(Kc prefactor); per pres_mod entry the Troe and
-  // SRI constants in multiply form; per species the 2x7 Gibbs
-  // coefficients; the 256-entry 2^(j/256) table of the exponential.
-  int rate_x, kc_lpref, troe_x, sri_x, sp_gibbs, exptab;
-  // derived f32 sections (mixed kernel): per rate row ln|A|, b, -Ta as
-  // float-float pairs and sign(A); 1/mw; Troe and SRI constants (exponent
-  // factors as float-float pairs); efficiencies minus one.
-  int rate_ff, inv_mw_f, troe_ff, sri_ff, eff_f;
-  // derived f64 section (mixed, one state per thread): per reversible
-  // reaction 16 doubles [T_common, 0, lo c0..c6, hi c0..c6] of its Kc
-  // exponent polynomial with ln(prefactor) folded into c0; built when every
-  // reaction has a single T_common group (kc_single = 1)
-  int kc_poly, kc_single;
-  // derived sections (mixed, one state per thread): the net-nu species as
-  // int16 and each nu as the high word of its double (nu_hi_exact = 1 when
-  // every nu's low word is zero, i.e. the pair is exact)
-  int nu_sp16, nu_hi, nu_hi_exact;
-  // derived f64 section (thermo utilities): per species 24 doubles
-  // [RU/mw, mw, T_common, 0, lo: a0..a5, a1/2, a2/3, a3/4, a4/5, hi: same]
-  int sp_thermo;
-  // derived i32 sections: reaction processing order, start of each shape
-  // group in it (crs_shapes.cuh), expanded reactant / product factors
-  int perm, seg, rfac, pfac;
-  // warp-per-state kernels: reaction order (dperm), species-major net-nu
-  // CSR in reaction order (spc_ptr/spc_r/spc_nu), species per lane
-  // (lane_ptr/lane_sp)
-  int dperm, spc_ptr, spc_r, spc_nu, lane_ptr, lane_sp;
-  // f64 sections
-  int inv_mw, rate_par, rx_nu, px_nu, kc_tmid, kc_lo, kc_hi, kc_pref,
-      pm_eff_val, pm_troe, pm_sri, nu_val, sp_tmid, sp_lo, sp_hi, kc_dnu, sp_mw;
-  // PLOG and Chebyshev rate forms: per rate row an index into their tables
-  // (rate_aux), PLOG points (printed pressure, ln P, ln-P spacing, rate row)
-  // and Chebyshev coefficient blocks with their reduced-T/P constants
-  int rate_aux, plog_ptr, plog_row, plog_p, plog_lp, plog_dlp, cheb_ptr, cheb_nt, cheb_np,
-      cheb_par, cheb_tp;
-  // i32 sections
-  int rate_kind, rate_npow, rx_ptr, rx_sp, rx_nint, px_ptr, px_sp, px_nint,
-      rev_idx, kc_ptr, pm_idx, pm_kind, pm_form, pm_sp, pm_eff_ptr,
-      pm_eff_sp, pm_k0, pm_kinf, pm_troe_t2, pm_sri_de, nu_ptr, nu_sp;
-};
-
-// Typed view of an image (in shared or global memory).
-struct Tab {
-  const int32_t *perm, *seg;
-  const int16_t *rfac, *pfac;
-  const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
-  const double *spc_nu;
-  const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
-  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly, *sp_thermo;
-  int kc_single;
-  const int16_t *nu_sp16;
-  const int32_t *nu_hi;
-  const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
-      *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
-      *sp_hi, *kc_dnu, *sp_mw;
-  const int32_t *rate_aux, *plog_ptr, *plog_row, *cheb_ptr, *cheb_nt, *cheb_np;
-  const double *plog_p, *plog_lp, *plog_dlp, *cheb_par, *cheb_tp;
-  const int32_t *rate_kind, *rate_npow, *rx_ptr, *rx_sp, *rx_nint, *px_ptr,
-      *px_sp, *px_nint, *rev_idx, *kc_ptr, *pm_idx, *pm_kind, *pm_form,
-      *pm_sp, *pm_eff_ptr, *pm_eff_sp, *pm_k0, *pm_kinf, *pm_troe_t2,
-      *pm_sri_de, *nu_ptr, *nu_sp;
-  int N, R, NREV, NPM;
-};
-
-// View of an image whose byte ranges [lo, hi) and [lo2, hi2) have been
-// copied back to back to `near` (shared memory); every other section is
-// read at `far` (global memory).
-__host__ __device__ inline Tab make_tab2(const unsigned char *near,
-                                         const unsigned char *far,
-                                         const ImgLayout &L, int lo, int hi,
-                                         int lo2 = 0, int hi2 = 0) {
-  Tab t;
-#define CRS_P(x)                                                      \
-  ((L.x >= lo && L.x < hi)     ? near + (L.x - lo)                    \
-   : (L.x >= lo2 && L.x < hi2) ? near + (hi - lo) + (L.x - lo2)       \
-                               : far + L.x)
-#define CRS_F(x) t.x = reinterpret_cast<const double *>(CRS_P(x))
-#define CRS_S(x) t.x = reinterpret_cast<const float *>(CRS_P(x))
-#define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
-  CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
-  CRS_F(exptab); CRS_F(kc_poly); CRS_F(sp_thermo);
-  CRS_I(perm); CRS_I(seg);
-  t.rfac = reinterpret_cast<const int16_t *>(CRS_P(rfac));
-  t.pfac = reinterpret_cast<const int16_t *>(CRS_P(pfac));
-  t.nu_sp16 = reinterpret_cast<const int16_t *>(CRS_P(nu_sp16));
-  CRS_I(nu_hi);
-  CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
-  CRS_F(spc_nu);
-  CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
-  CRS_F(inv_mw); CRS_F(rate_par); CRS_F(rx_nu); CRS_F(px_nu); CRS_F(kc_tmid);
-  CRS_F(kc_lo); CRS_F(kc_hi); CRS_F(kc_pref); CRS_F(pm_eff_val);
-  CRS_F(pm_troe); CRS_F(pm_sri); CRS_F(nu_val); CRS_F(sp_tmid); CRS_F(sp_lo);
-  CRS_F(sp_hi); CRS_F(kc_dnu); CRS_F(sp_mw);
-  CRS_I(rate_aux); CRS_I(plog_ptr); CRS_I(plog_row); CRS_I(cheb_ptr); CRS_I(cheb_nt);
-  CRS_I(cheb_np); CRS_F(plog_p); CRS_F(plog_lp); CRS_F(plog_dlp); CRS_F(cheb_par);
-  CRS_F(cheb_tp);
-  CRS_I(rate_kind); CRS_I(rate_npow); CRS_I(rx_ptr); CRS_I(rx_sp);
-  CRS_I(rx_nint); CRS_I(px_ptr); CRS_I(px_sp); CRS_I(px_nint); CRS_I(rev_idx);
-  CRS_I(kc_ptr); CRS_I(pm_idx); CRS_I(pm_kind); CRS_I(pm_form); CRS_I(pm_sp);
-  CRS_I(pm_eff_ptr); CRS_I(pm_eff_sp); CRS_I(pm_k0); CRS_I(pm_kinf);
-  CRS_I(pm_troe_t2); CRS_I(pm_sri_de); CRS_I(nu_ptr); CRS_I(nu_sp);
-#undef CRS_P
-#undef CRS_F
-#undef CRS_S
-#undef CRS_I
-  t.N = L.N; t.R = L.R; t.NREV = L.NREV; t.NPM = L.NPM;
-  t.kc_single = L.kc_single;
-  return t;
-}
-
-__host__ __device__ inline Tab make_tab(const unsigned char *b,
-                                        const ImgLayout &L) {
-  return make_tab2(b, b, L, 0, 0);
-}
 
 namespace mixed {
 // Output of the mixed rates-only kernel that feeds the tensor-core
@@ -323,80 +191,9 @@ cudaError_t launch_dydt_finish(const unsigned char *img, const ImgLayout &L, int
                                int64_t n, const double *y, int64_t ld, const double *p_or_rho,
                                const double *W, double *dy, int sm_count, cudaStream_t s);
 
-#ifdef __CUDACC__
-// rxn_rate_const in the emitted form (rate_subs.py:60-135), CUDA exp.
-__device__ inline double ref_rate_const(const Tab &t, int row, double T, double logT) {
-  const double *p = t.rate_par + 4 * row;  // A, logA, b, Ta
-  switch (t.rate_kind[row]) {
-    case RATE_CONST:
-      return p[0];
-    case RATE_EXP:
-      return exp(p[1] + p[2] * logT - (p[3] / T));
-    case RATE_NEGEXP:
-      return p[0] * exp(p[2] * logT - (p[3] / T));
-    default: {
-      double k = p[0];
-      for (int j = 0; j < t.rate_npow[row]; ++j) k = k * T;
-      return k;
-    }
-  }
-}
-
-// Forward rate constant of a PLOG row (rate_subs.py:444-485: branch
-// thresholds as printed with %.4e, log-linear interpolation in ln P between
-// the bracketing points) or a Chebyshev row (rate_subs.py:136-223: reduced
-// temperature and pressure, the pressure dot products by the Chebyshev
-// recursion, then the temperature sum, 10^kf), in the emitted order.
-__device__ inline double pdep_kf(const Tab &t, int row, double T, double logT, double pres) {
-  const int a = t.rate_aux[row];
-  if (t.rate_kind[row] == RATE_PLOG) {
-    const int e0 = t.plog_ptr[a], e1 = t.plog_ptr[a + 1];
-    if (pres <= t.plog_p[e0]) return ref_rate_const(t, t.plog_row[e0], T, logT);
-    for (int e = e0; e < e1 - 1; ++e)
-      if ((pres > t.plog_p[e]) && (pres <= t.plog_p[e + 1])) {
-        const double k1 = log(ref_rate_const(t, t.plog_row[e], T, logT));
-        const double k2 = log(ref_rate_const(t, t.plog_row[e + 1], T, logT));
-        return exp(k1 + (k2 - k1) * (log(pres) - t.plog_lp[e]) / t.plog_dlp[e]);
-      }
-    if (pres > t.plog_p[e1 - 1]) return ref_rate_const(t, t.plog_row[e1 - 1], T, logT);
-    return __longlong_as_double(0x7ff8000000000000ll);  // no branch (NaN pressure)
-  }
-  const double *tp = t.cheb_tp + 4 * a;
-  const int nt = t.cheb_nt[a], np = t.cheb_np[a];
-  const double *c = t.cheb_par + t.cheb_ptr[a];  // [nt][np]
-  const double Tred = ((2.0 / T) - tp[0]) / tp[1];
-  const double Pred = (2.0 * log10(pres) - tp[2]) / tp[3];
-  double dp[CHEB_MAX];
-  for (int i = 0; i < nt; ++i) dp[i] = c[i * np] + Pred * c[i * np + 1];
-  double ct0 = 1.0, ct1 = Pred;
-  bool upd = true;
-  for (int j = 2; j < np; ++j) {
-    if (upd) {
-      ct0 = 2.0 * Pred * ct1 - ct0;
-      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct0;
-    } else {
-      ct1 = 2.0 * Pred * ct0 - ct1;
-      for (int i = 0; i < nt; ++i) dp[i] += c[i * np + j] * ct1;
-    }
-    upd = !upd;
-  }
-  ct0 = 1.0;
-  ct1 = Tred;
-  double kf = dp[0] + Tred * dp[1];
-  upd = true;
-  for (int i = 2; i < nt; ++i) {
-    if (upd) {
-      ct0 = 2.0 * Tred * ct1 - ct0;
-      kf += dp[i] * ct0;
-    } else {
-      ct1 = 2.0 * Tred * ct0 - ct1;
-      kf += dp[i] * ct1;
-    }
-    upd = !upd;
-  }
-  return pow(10.0, kf);
-}
-#endif
+// The PLOG / Chebyshev forward rate constant in the emitted order, shared
+// by every kernel (these reactions are rare; FP64 in every mode).
+using ref::pdep_kf;
 
 #ifdef __CUDACC__
 // Exponent of the equilibrium constant of reversible reaction j (with ln

@@ -684,19 +684,25 @@ __global__ void __launch_bounds__(DW * 32)
       s.iTff = ff_from_double(s.invT);
       const double P = bP[j];
       s.P = P;
-      double ys = 0.0, mw = 0.0;
+      double mw = 0.0;
       for (int k = lane; k < N - 1; k += 32) {
         const double y = b.Y[(int64_t)k * b.ld + i];
-        ys += y;
+        S[k] = y;  // parked in the Gibbs column until C is formed
         mw = fma(y, t.inv_mw[k], mw);
       }
-      ys = warp_sum(ys);
       mw = warp_sum(mw);
+      __syncwarp();
+      // y_N = 1 - sum y in the reference's left-to-right order on every
+      // lane (rate_subs.py:1312-1320): where the bath gas is scarce, the
+      // rounding of this difference is a large relative error of C_N
+      double ys = N > 1 ? S[0] : 0.0;
+      for (int k = 1; k < N - 1; ++k) ys += S[k];
       const double yN = 1.0 - ys;
       mw = fma(yN, t.inv_mw[N - 1], mw);
       const double rho = P / mw * (s.invT * INV_RU);
+      __syncwarp();  // every lane has read the parked y before any is replaced
       for (int k = lane; k < N; k += 32) {
-        const double y = (k == N - 1) ? yN : b.Y[(int64_t)k * b.ld + i];
+        const double y = (k == N - 1) ? yN : S[k];
         const float c = d2f_rn(y * (rho * t.inv_mw[k]));
         C[k] = c;
         if (STAGES && b.conc) b.conc[(int64_t)k * b.ld + i] = (double)c;

@@ -45,7 +45,7 @@ typedef struct crs_mech crs_mech;
 #define CRS_ERR_CUDA 3        /* CUDA runtime error (text in crs_last_error) */
 #define CRS_ERR_UNSUPPORTED 4 /* mode not available for this mechanism */
 #define CRS_ERR_TIMEOUT 5     /* a bounded device or host wait expired */
-#define CRS_ERR_NOMECH 6      /* per-state call without crs_bind */
+#define CRS_ERR_NOMECH 6      /* per-state call without a bound mechanism */
 
 /* Evaluation modes of crs_wdot. */
 #define CRS_MODE_FP64 0        /* FP64 throughout; <=1e-12 of the reference */
@@ -307,12 +307,36 @@ int crs_scatter_wdot(int64_t m, const int64_t *idx, const double *Wc,
 
 /* ---- per-state drop-in (the reference's emitted signatures) ----------- */
 
-/* Select the mechanism used by the four functions below (NULL unbinds).
- * They take HOST pointers, run one state through the same GPU kernels on
- * the legacy default stream and return when the result is on the host.
- * They are serialised by a process-wide lock.  Failures leave NaN in the
- * outputs and a message in crs_last_error(). */
+/* The reference emits these as pure host functions with the mechanism
+ * compiled in; an integrator calls them once per state, often from many
+ * OpenMP threads.  Here they evaluate a mechanism's host table image on the
+ * calling thread in FP64, in the reference's operation order
+ * (include/crs_eval.h, compiled without floating-point contraction): the
+ * results equal the emitted C's bit for bit.  They lock nothing, launch
+ * nothing, need no GPU, and may run on any number of threads at once.
+ *
+ * The mechanism is the calling thread's own binding (crs_bind_thread) when
+ * it has one, else the process-wide binding (crs_bind).  A handle must stay
+ * loaded while calls may use it; crs_mech_free removes it from the
+ * process-wide binding and from the calling thread's.  Without a binding
+ * the outputs are left untouched and crs_last_error() says so. */
+
+/* Host-only load: the table image for the per-state functions and the
+ * crs_state_* calls, without a GPU.  Batched entry points refuse such a
+ * handle (CRS_ERR_ARG).  Free with crs_mech_free. */
+int crs_mech_load_host(const void *blob, size_t nbytes, crs_mech **out);
+/* The table image of a blob (host only), for code that compiles it into a
+ * program (the per-state device functions of include/crs_device.cuh):
+ * sizes[0] = image bytes, sizes[1] = int32 words of crs::ImgLayout
+ * (include/crs_tables.h).  img / layout may be NULL (sizes only); else they
+ * receive the image and the layout words. */
+int crs_mech_image(const void *blob, size_t nbytes, void *img, size_t img_cap,
+                   int32_t *layout, size_t layout_cap, size_t sizes[2]);
+/* Process-wide mechanism of the functions below (NULL unbinds). */
 int crs_bind(const crs_mech *mech);
+/* The calling thread's own mechanism, ahead of the process-wide one (NULL
+ * returns the thread to the process-wide binding). */
+int crs_bind_thread(const crs_mech *mech);
 
 /* rate_subs.py:1297-1299 (chem_utils.h) */
 void eval_conc(const double T, const double pres, const double *y,
@@ -338,10 +362,31 @@ void eval_conc_rho(const double T, const double rho, const double *y,
 /* rate_subs.py:1829-2067 (dydt.h): y = [T, Y_0 .. Y_{N-2}], dy the same;
  * `pres` is the pressure (constant pressure, the default) or the density
  * after crs_dydt_form(1) (constant volume), as the emitted -DCONP / -DCONV
- * builds read it.  Uses CRS_MODE_FP64_STRICT for wdot. */
+ * builds read it.  The constant-volume form takes the pressure and the
+ * concentrations from eval_conc_rho (the reference's constant-volume text
+ * does not compile, rate_subs.py:1967-1969, 2024-2025). */
 void dydt(const double t, const double pres, const double *y, double *dy);
-/* Form of the per-state dydt: 0 constant pressure, 1 constant volume. */
+/* Form of the per-state dydt, process-wide: 0 constant pressure, 1
+ * constant volume. */
 int crs_dydt_form(int conv);
+
+/* The same functions with the mechanism passed explicitly (no binding) and
+ * an error code returned: CRS_ERR_ARG for a NULL handle or array. */
+int crs_state_eval_conc(const crs_mech *mech, double T, double pres, const double *y,
+                        double *y_N, double *mw_avg, double *rho, double *conc);
+int crs_state_eval_rxn_rates(const crs_mech *mech, double T, double pres, const double *C,
+                             double *fwd, double *rev);
+int crs_state_get_rxn_pres_mod(const crs_mech *mech, double T, double pres,
+                               const double *C, double *pres_mod);
+int crs_state_eval_spec_rates(const crs_mech *mech, const double *fwd, const double *rev,
+                              const double *pres_mod, double *sp_rates, double *dy_N);
+/* which: 0 h, 1 u, 2 cv, 3 cp; out [N] */
+int crs_state_eval_thermo(const crs_mech *mech, int which, double T, double *out);
+int crs_state_eval_conc_rho(const crs_mech *mech, double T, double rho, const double *y,
+                            double *y_N, double *mw_avg, double *pres, double *conc);
+/* conv 0: p_or_rho = P (constant pressure); 1: p_or_rho = rho */
+int crs_state_dydt(const crs_mech *mech, int conv, double p_or_rho, const double *y,
+                   double *dy);
 
 #ifdef __cplusplus
 }
