@@ -43,6 +43,18 @@ cudaError_t launch_gemm_wdot(const void *A, const void *B, int64_t M_pad, int64_
                              int64_t K, int block_n, double *out, int64_t ld, int m_valid,
                              int n_valid, const int *escale, int32_t *status,
                              cudaStream_t s);
+// Mixed precision for large mechanisms in two passes over HBM (crs_large.cu).
+size_t large_rates_smem(const ImgLayout &L);
+cudaError_t launch_rates_tile(const unsigned char *img, const ImgLayout &L, const Batch &b,
+                              int sm_count, int smem_optin, cudaStream_t s, double *q,
+                              int64_t ldq, int *escale);
+cudaError_t launch_spec_sum(const unsigned char *img, const ImgLayout &L, const double *q,
+                            int64_t ldq, int64_t n, const int *escale, bool outwin,
+                            double *wdot, int64_t ld, int32_t *status, int sm_count,
+                            cudaStream_t s);
+cudaError_t launch_pack_bf16(const double *q, int64_t ldq, int64_t n, int R, int Kh,
+                             const int *escale, void *A, int64_t lda, int sm_count,
+                             cudaStream_t s);
 // Tables the fast kernels derive from the blob's tables at load time.
 bool build_fast_tables(const std::vector<unsigned char> &img,
                        const ImgLayout &L, std::vector<Derived> &extra);
@@ -91,6 +103,14 @@ struct crs_mech {
   void *d_ws = nullptr;
   int *d_escale = nullptr;
   int64_t ws_rows = 0;
+  // two-pass mixed precision of large mechanisms (and the contraction's
+  // producer): FP64 net rates of one chunk of states [R][q_rows]
+  double *d_q = nullptr;
+  int64_t q_rows = 0;
+  // recorded after the last kernel that used the workspaces, waited on by
+  // the next call's stream: calls on several streams take turns on the GPU
+  cudaEvent_t ws_done = nullptr;
+  bool ws_used = false;
   // crs_wdot_host: two streams and two device buffers of one chunk of
   // states each (T, P, Y, wdot), allocated on first use
   std::mutex host_mu;
@@ -453,7 +473,7 @@ crs::Batch make_batch(const crs_mech *m, int64_t n, int64_t ld) {
 }
 
 // Chunk of states per contraction pass (workspace rows).
-constexpr int64_t GEMM_CHUNK = 1 << 18;
+constexpr int64_t GEMM_CHUNK = 1 << 17;
 
 int gemm_prepare(crs_mech *m) {
   if (m->gemm_state) return m->gemm_state > 0 ? CRS_OK : CRS_ERR_UNSUPPORTED;
@@ -485,42 +505,139 @@ int gemm_prepare(crs_mech *m) {
   return CRS_OK;
 }
 
-int wdot_gemm(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
-  std::lock_guard<std::mutex> lk(m->ws_mu);
-  int rc = gemm_prepare(m);
-  if (rc != CRS_OK) return rc;
-  const int64_t K = 2 * (int64_t)m->Kh;
-  const int64_t rows = std::min<int64_t>((b.n + 127) / 128 * 128, GEMM_CHUNK);
-  if (m->ws_rows < rows) {
+// Largest chunk of states whose FP64 net rates fit in ~2 GiB (a multiple
+// of 128, at most GEMM_CHUNK).
+int64_t q_chunk(const crs::ImgLayout &L, int64_t n) {
+  int64_t c = ((int64_t)2 << 30) / ((int64_t)8 * (L.R > 0 ? L.R : 1));
+  c = std::min<int64_t>(c, GEMM_CHUNK) / 128 * 128;
+  if (c < 128) c = 128;
+  return std::min<int64_t>(c, (n + 127) / 128 * 128);
+}
+
+// Workspace of the two-pass paths for chunks of `rows` states (caller
+// holds ws_mu); with_ws: also the contraction's bf16 rows and exponents.
+int ensure_q(crs_mech *m, int64_t rows, bool with_ws) {
+  cudaError_t e = cudaSuccess;
+  if (m->q_rows < rows) {
+    if (m->d_q) cudaFree(m->d_q);
+    m->d_q = nullptr;
+    m->q_rows = 0;
+    e = cudaMalloc(&m->d_q, (size_t)rows * (m->L.R > 0 ? m->L.R : 1) * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "rates workspace");
+    m->q_rows = rows;
+  }
+  if (with_ws && m->ws_rows < rows) {
     if (m->d_ws) cudaFree(m->d_ws);
     if (m->d_escale) cudaFree(m->d_escale);
     m->d_ws = nullptr;
     m->d_escale = nullptr;
     m->ws_rows = 0;
-    cudaError_t e = cudaMalloc(&m->d_ws, (size_t)rows * K * sizeof(__nv_bfloat16));
+    const int64_t K = 2 * (int64_t)m->Kh;
+    e = cudaMalloc(&m->d_ws, (size_t)rows * K * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&m->d_escale, (size_t)rows * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "gemm workspace");
     m->ws_rows = rows;
   }
-  for (int64_t c0 = 0; c0 < b.n; c0 += m->ws_rows) {
-    const int64_t cnt = std::min<int64_t>(m->ws_rows, b.n - c0);
+  if (!m->ws_done) {
+    e = cudaEventCreateWithFlags(&m->ws_done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "workspace event");
+  }
+  return CRS_OK;
+}
+
+// Order this call's use of the workspaces after the previous call's, on
+// whatever stream that ran (not while the stream is being captured into a
+// graph, where the caller orders the work).
+int ws_begin(crs_mech *m, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return cuda_fail(e, "workspace ordering");
+  if (m->ws_used && cs == cudaStreamCaptureStatusNone) {
+    e = cudaStreamWaitEvent(s, m->ws_done, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "workspace ordering");
+  }
+  return CRS_OK;
+}
+
+int ws_end(crs_mech *m, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+    e = cudaEventRecord(m->ws_done, s);
+    m->ws_used = e == cudaSuccess;
+  }
+  return e == cudaSuccess ? CRS_OK : cuda_fail(e, "workspace ordering");
+}
+
+// Mixed precision in two passes (large mechanisms): per chunk, the
+// state-tile rates kernel writes the FP64 net rates, the species sums read
+// them.
+int wdot_two_pass(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
+  if ((size_t)crs::large_rates_smem(m->L) > (size_t)m->smem_optin)
+    return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates tile");
+  std::lock_guard<std::mutex> lk(m->ws_mu);
+  const int64_t rows = q_chunk(m->L, b.n);
+  int rc = ensure_q(m, rows, false);
+  if (rc == CRS_OK) rc = ws_begin(m, s);
+  if (rc != CRS_OK) return rc;
+  for (int64_t c0 = 0; c0 < b.n && rc == CRS_OK; c0 += rows) {
+    const int64_t cnt = std::min<int64_t>(rows, b.n - c0);
+    crs::Batch bc = b;
+    bc.n = cnt;
+    bc.T = b.T + c0;
+    bc.P = b.P + c0;
+    bc.Y = b.Y + c0;
+    cudaError_t e = crs::launch_rates_tile(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
+                                           m->d_q, rows, nullptr);
+    if (e == cudaSuccess)
+      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, nullptr, false, b.wdot + c0,
+                               b.ld, m->d_status, m->sm_count, s);
+    if (e == cudaErrorNotSupported) rc = fail(CRS_ERR_UNSUPPORTED, "rates tile not available");
+    else if (e != cudaSuccess) rc = cuda_fail(e, "two-pass mixed launch");
+  }
+  const int rc2 = ws_end(m, s);
+  return rc != CRS_OK ? rc : rc2;
+}
+
+// CRS_MODE_GEMM: per chunk, the FP64 net rates (state tiles), their bf16
+// hi + lo rows scaled per state, the terms outside the bf16 window summed
+// in FP64 into wdot, and the contraction GEMM adding the rest.
+int wdot_gemm(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
+  if ((size_t)crs::large_rates_smem(m->L) > (size_t)m->smem_optin)
+    return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates tile");
+  std::lock_guard<std::mutex> lk(m->ws_mu);
+  int rc = gemm_prepare(m);
+  if (rc != CRS_OK) return rc;
+  const int64_t K = 2 * (int64_t)m->Kh;
+  const int64_t rows = q_chunk(m->L, b.n);
+  rc = ensure_q(m, rows, true);
+  if (rc == CRS_OK) rc = ws_begin(m, s);
+  if (rc != CRS_OK) return rc;
+  for (int64_t c0 = 0; c0 < b.n && rc == CRS_OK; c0 += rows) {
+    const int64_t cnt = std::min<int64_t>(rows, b.n - c0);
     crs::Batch bc = b;
     bc.n = cnt;
     bc.T = b.T + c0;
     bc.P = b.P + c0;
     bc.Y = b.Y + c0;
     bc.wdot = b.wdot + c0;
-    crs::mixed::QOut qo{m->d_ws, K, m->Kh, m->d_escale};
-    cudaError_t e = crs::launch_wdot_mixed_q(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s, qo);
-    if (e == cudaErrorNotSupported)
-      return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates kernel");
-    if (e != cudaSuccess) return cuda_fail(e, "gemm rates launch");
+    cudaError_t e = crs::launch_rates_tile(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
+                                           m->d_q, rows, m->d_escale);
+    if (e == cudaSuccess)
+      e = crs::launch_pack_bf16(m->d_q, rows, cnt, m->L.R, m->Kh, m->d_escale, m->d_ws, K,
+                                m->sm_count, s);
+    if (e == cudaSuccess)
+      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, m->d_escale, true, bc.wdot,
+                               b.ld, m->d_status, m->sm_count, s);
     const int64_t M_pad = (cnt + 127) / 128 * 128;
-    e = crs::launch_gemm_wdot(m->d_ws, m->d_nuB, M_pad, m->N_pad, K, m->block_n, bc.wdot, b.ld,
-                              (int)cnt, m->L.N, m->d_escale, m->d_status, s);
-    if (e != cudaSuccess) return cuda_fail(e, "gemm contraction launch");
+    if (e == cudaSuccess)
+      e = crs::launch_gemm_wdot(m->d_ws, m->d_nuB, M_pad, m->N_pad, K, m->block_n, bc.wdot,
+                                b.ld, (int)cnt, m->L.N, m->d_escale, m->d_status, s);
+    if (e == cudaErrorNotSupported) rc = fail(CRS_ERR_UNSUPPORTED, "rates tile not available");
+    else if (e != cudaSuccess) rc = cuda_fail(e, "gemm launch");
   }
-  return CRS_OK;
+  const int rc2 = ws_end(m, s);
+  return rc != CRS_OK ? rc : rc2;
 }
 
 }  // namespace
@@ -541,11 +658,20 @@ int launch_mode(const crs_mech *m, crs::Batch &b, int mode, cudaStream_t s) {
         e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_MIXED:
-      // one state per thread when its columns fit on chip, else per warp
+      // one state per thread when its columns fit on chip; else the
+      // two-pass state-tile path (per warp when intermediates are asked for)
       e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      if (e == cudaErrorNotSupported)
+      if (e == cudaErrorNotSupported) {
+        if (!(b.conc || b.fwd || b.rev || b.pm) &&
+            crs::large_rates_smem(m->L) <= (size_t)m->smem_optin)
+          return wdot_two_pass(const_cast<crs_mech *>(m), b, s);
         e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      }
       break;
+    case CRS_MODE_MIXED_TILE:
+      if (b.conc || b.fwd || b.rev || b.pm)
+        return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_MIXED_TILE does not write intermediates");
+      return wdot_two_pass(const_cast<crs_mech *>(m), b, s);
     case CRS_MODE_FP64_TPS:
       e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
@@ -688,6 +814,8 @@ int crs_mech_free(crs_mech *m) {
   if (m->d_nuB) cudaFree(m->d_nuB);
   if (m->d_ws) cudaFree(m->d_ws);
   if (m->d_escale) cudaFree(m->d_escale);
+  if (m->d_q) cudaFree(m->d_q);
+  if (m->ws_done) cudaEventDestroy(m->ws_done);
   if (m->d_host) cudaFree(m->d_host);
   for (cudaStream_t st : m->hs)
     if (st) cudaStreamDestroy(st);

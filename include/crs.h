@@ -65,10 +65,18 @@ typedef struct crs_mech crs_mech;
 /* Mixed-precision rates, then the stoichiometric contraction
  * wdot = q . nu as a BF16 tensor-core GEMM (q split into bf16 hi + lo,
  * scaled per state; terms far outside the scale summed in FP64; FP32
- * accumulation).  For large mechanisms.  Uses a workspace owned by the
- * handle (allocated on first use, <= 2^18 states x 4 x R_pad bytes);
- * calls on one handle are serialised.  No intermediates. */
+ * accumulation).  For large mechanisms.  No intermediates. */
 #define CRS_MODE_GEMM 7
+/* The arithmetic of CRS_MODE_MIXED in two passes: net rates of tiles of 32
+ * states (all warps of a CTA on one tile) to HBM in FP64, then the species
+ * sums.  CRS_MODE_MIXED takes this path when a mechanism's per-thread
+ * columns do not fit on chip and no intermediates are asked for.  No
+ * intermediates.
+ * CRS_MODE_GEMM and the two-pass path use a workspace owned by the handle,
+ * allocated on first use (FP64 rates of up to 2^17 states, <= ~2 GiB, plus
+ * 4 bytes per reaction and state for the contraction): calls on one handle
+ * take turns on the GPU, whatever their streams. */
+#define CRS_MODE_MIXED_TILE 8
 
 /* ---- mechanism tables ------------------------------------------------ */
 

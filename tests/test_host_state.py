@@ -125,6 +125,27 @@ def test_reference_signatures_bitexact_vs_golden(case, golden):
 
 
 @pytest.mark.parametrize("case", ["gri53", "features"])
+def test_constant_volume_dydt_equals_the_oracle(case, golden):
+    """Constant volume (whose emitted text does not compile in the
+    reference) against the oracle's restatement, bit for bit."""
+    from oracle.oracle import Oracle
+    mech, g = golden(case)
+    hm = HostMech(mech)
+    N = mech.n_species
+    ys = np.concatenate([g["T"][None], g["Y"][: N - 1]], axis=0)
+    rho = g["misc"][2]
+    want = Oracle(mech.blob).dydt(rho, ys, conv=True)
+    try:
+        for i in range(g["T"].shape[0]):
+            y = np.ascontiguousarray(ys[:, i])
+            dy = np.zeros(N)
+            _lib.check(hm.lib.crs_state_dydt(hm.h, 1, float(rho[i]), dp(y), dp(dy)))
+            assert np.array_equal(dy, want[:, i]), (case, i)
+    finally:
+        hm.close()
+
+
+@pytest.mark.parametrize("case", ["gri53", "features"])
 def test_explicit_handle_calls_bitexact_vs_golden(case, golden):
     mech, g = golden(case)
     hm = HostMech(mech)
