@@ -61,6 +61,9 @@ def _args():
                          "(the case of the network-kernel ncu summary)")
     ap.add_argument("--profile", action="store_true",
                     help="one launch of each wdot kernel on 2^18 states (for ncu)")
+    ap.add_argument("--profile-large", action="store_true",
+                    help="one evaluation per mode of the 561-species mechanism on 2^16 "
+                         "states (for ncu)")
     return ap.parse_args()
 
 
@@ -757,6 +760,29 @@ def run_profile(args):
     return 0
 
 
+def run_profile_large(args):
+    """One evaluation per large-mechanism mode on 2^16 states: the case of
+    the rates-tile ncu summary."""
+    import torch
+    from create_rate_subs_gb300 import synth
+    from create_rate_subs_gb300.mechanism import Mechanism
+    from create_rate_subs_gb300.rates import RateSubs
+    torch.cuda.set_device(0)
+    d = tempfile.mkdtemp(prefix="crs_prof_large_")
+    mech = Mechanism.from_chemkin(*synth.write_mechanism("large561", d))
+    rs = RateSubs(mech)
+    n = 1 << 16
+    T, P, Y = synth.make_states(mech.n_species, n, seed=5)
+    dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[:-1].copy()))
+    out = torch.empty((mech.n_species, n), dtype=torch.float64, device="cuda")
+    for mode in ("mixed", "gemm"):
+        rs.wdot(dT, dP, dY, mode, out=out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "large561, %d states, one evaluation per mode" % n,
+                      "status": rs.status()}))
+    return 0
+
+
 def run_profile_surrogate(args):
     """Features, the four layer GEMMs and the output kernel of the surrogate
     network (random weights) over 2^20 states, once."""
@@ -781,6 +807,8 @@ def main():
         return run_profile(args)
     if args.profile_surrogate:
         return run_profile_surrogate(args)
+    if args.profile_large:
+        return run_profile_large(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

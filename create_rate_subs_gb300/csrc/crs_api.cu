@@ -49,12 +49,12 @@ cudaError_t launch_rates_tile(const unsigned char *img, const ImgLayout &L, cons
                               int sm_count, int smem_optin, cudaStream_t s, double *q,
                               int64_t ldq, int *escale);
 cudaError_t launch_spec_sum(const unsigned char *img, const ImgLayout &L, const double *q,
-                            int64_t ldq, int64_t n, const int *escale, bool outwin,
+                            int64_t ldq, int64_t n, const int *escale, const unsigned *outflag,
                             double *wdot, int64_t ld, int32_t *status, int sm_count,
                             cudaStream_t s);
 cudaError_t launch_pack_bf16(const double *q, int64_t ldq, int64_t n, int R, int Kh,
-                             const int *escale, void *A, int64_t lda, int sm_count,
-                             cudaStream_t s);
+                             const int *escale, void *A, int64_t lda, unsigned *outflag,
+                             int sm_count, cudaStream_t s);
 // Tables the fast kernels derive from the blob's tables at load time.
 bool build_fast_tables(const std::vector<unsigned char> &img,
                        const ImgLayout &L, std::vector<Derived> &extra);
@@ -102,6 +102,7 @@ struct crs_mech {
   void *d_nuB = nullptr;
   void *d_ws = nullptr;
   int *d_escale = nullptr;
+  unsigned *d_outflag = nullptr;  // states with terms outside the bf16 window
   int64_t ws_rows = 0;
   // two-pass mixed precision of large mechanisms (and the contraction's
   // producer): FP64 net rates of one chunk of states [R][q_rows]
@@ -529,12 +530,15 @@ int ensure_q(crs_mech *m, int64_t rows, bool with_ws) {
   if (with_ws && m->ws_rows < rows) {
     if (m->d_ws) cudaFree(m->d_ws);
     if (m->d_escale) cudaFree(m->d_escale);
+    if (m->d_outflag) cudaFree(m->d_outflag);
     m->d_ws = nullptr;
     m->d_escale = nullptr;
+    m->d_outflag = nullptr;
     m->ws_rows = 0;
     const int64_t K = 2 * (int64_t)m->Kh;
     e = cudaMalloc(&m->d_ws, (size_t)rows * K * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&m->d_escale, (size_t)rows * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_outflag, (size_t)rows * sizeof(unsigned));
     if (e != cudaSuccess) return cuda_fail(e, "gemm workspace");
     m->ws_rows = rows;
   }
@@ -590,8 +594,8 @@ int wdot_two_pass(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
     cudaError_t e = crs::launch_rates_tile(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
                                            m->d_q, rows, nullptr);
     if (e == cudaSuccess)
-      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, nullptr, false, b.wdot + c0,
-                               b.ld, m->d_status, m->sm_count, s);
+      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, nullptr, nullptr,
+                               b.wdot + c0, b.ld, m->d_status, m->sm_count, s);
     if (e == cudaErrorNotSupported) rc = fail(CRS_ERR_UNSUPPORTED, "rates tile not available");
     else if (e != cudaSuccess) rc = cuda_fail(e, "two-pass mixed launch");
   }
@@ -625,10 +629,10 @@ int wdot_gemm(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
                                            m->d_q, rows, m->d_escale);
     if (e == cudaSuccess)
       e = crs::launch_pack_bf16(m->d_q, rows, cnt, m->L.R, m->Kh, m->d_escale, m->d_ws, K,
-                                m->sm_count, s);
+                                m->d_outflag, m->sm_count, s);
     if (e == cudaSuccess)
-      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, m->d_escale, true, bc.wdot,
-                               b.ld, m->d_status, m->sm_count, s);
+      e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, m->d_escale, m->d_outflag,
+                               bc.wdot, b.ld, m->d_status, m->sm_count, s);
     const int64_t M_pad = (cnt + 127) / 128 * 128;
     if (e == cudaSuccess)
       e = crs::launch_gemm_wdot(m->d_ws, m->d_nuB, M_pad, m->N_pad, K, m->block_n, bc.wdot,
@@ -814,6 +818,7 @@ int crs_mech_free(crs_mech *m) {
   if (m->d_nuB) cudaFree(m->d_nuB);
   if (m->d_ws) cudaFree(m->d_ws);
   if (m->d_escale) cudaFree(m->d_escale);
+  if (m->d_outflag) cudaFree(m->d_outflag);
   if (m->d_q) cudaFree(m->d_q);
   if (m->ws_done) cudaEventDestroy(m->ws_done);
   if (m->d_host) cudaFree(m->d_host);

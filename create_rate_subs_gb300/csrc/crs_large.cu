@@ -184,8 +184,9 @@ __device__ __forceinline__ bool in_window(double v, int c) {
 template <bool OUTWIN>
 __global__ void __launch_bounds__(256)
     k_spec_sum(const unsigned char *__restrict__ img, ImgLayout L, const double *__restrict__ q,
-               int64_t ldq, int64_t n, const int *__restrict__ escale, double *__restrict__ wdot,
-               int64_t ld, int32_t *status) {
+               int64_t ldq, int64_t n, const int *__restrict__ escale,
+               const unsigned *__restrict__ outflag, double *__restrict__ wdot, int64_t ld,
+               int32_t *status) {
   const Tab t = make_tab(img, L);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   int bad = 0;
@@ -195,6 +196,13 @@ __global__ void __launch_bounds__(256)
     const int64_t ic = valid ? i : tile * 32;
     const int c = OUTWIN ? escale[ic] : 0;
     const double *qi = q + ic;
+    if (OUTWIN && !__any_sync(0xffffffffu, valid && outflag[ic] != 0u)) {
+      // no term of these states lies outside the window: the sums are zero
+      // (the contraction's epilogue adds the rest)
+      if (valid)
+        for (int k = warp; k < t.N; k += nw) wdot[(int64_t)k * ld + i] = 0.0;
+      continue;
+    }
     for (int k = warp; k < t.N; k += nw) {
       double w = 0.0;
       const int e1 = t.spc_ptr[k + 1];
@@ -222,13 +230,14 @@ __global__ void __launch_bounds__(256)
 }
 
 // A[i][r] = bf16 hi of q[r][i] * 2^-c_i, A[i][Kh + r] = bf16 lo, for the
-// terms within the window (others 0: k_spec_sum<true> sums them in FP64);
-// columns R..Kh-1 zero.  CTA: 32 states x 64 reactions through shared
+// terms within the window (others 0: k_spec_sum<true> sums them in FP64,
+// and outflag[i], zero on entry, marks state i); columns R..Kh-1 zero.  CTA: 32 states x 64 reactions through shared
 // memory, so that both the reads (256 B per reaction row) and the writes
 // (128 B per state row) are contiguous.
 __global__ void __launch_bounds__(256)
     k_pack_bf16(const double *__restrict__ q, int64_t ldq, int64_t n, int R, int Kh,
-                const int *__restrict__ escale, __nv_bfloat16 *__restrict__ A, int64_t lda) {
+                const int *__restrict__ escale, __nv_bfloat16 *__restrict__ A, int64_t lda,
+                unsigned *__restrict__ outflag) {
   __shared__ float f[64][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t ntile = (n + 31) / 32;
@@ -243,7 +252,8 @@ __global__ void __launch_bounds__(256)
       const int r = r0 + rr;
       const double v = (valid && r < R) ? q[(int64_t)r * ldq + i] : 0.0;
       float x = 0.0f;
-      if (in_window(v, c) && v != 0.0) {
+      if (!in_window(v, c)) atomicOr(&outflag[i], 1u);  // rare: marks the state
+      else if (v != 0.0) {
         const int hi = __double2hiint(v), lo = __double2loint(v);
         // v * 2^-c exactly through the exponent field (the result stays a
         // normal number within 2^+-WINDOW), then rounded to fp32
@@ -297,27 +307,34 @@ cudaError_t launch_rates_tile(const unsigned char *img, const ImgLayout &L, cons
   return cudaGetLastError();
 }
 
+// outflag: NULL for the full sums; else the per-state marks of
+// k_pack_bf16, and only the terms outside the window are summed.
 cudaError_t launch_spec_sum(const unsigned char *img, const ImgLayout &L, const double *q,
-                            int64_t ldq, int64_t n, const int *escale, bool outwin,
+                            int64_t ldq, int64_t n, const int *escale, const unsigned *outflag,
                             double *wdot, int64_t ld, int32_t *status, int sm_count,
                             cudaStream_t s) {
   const int64_t ntiles = (n + 31) / 32;
   const int grid = grid_for(ntiles, 1, sm_count * 8);
-  if (outwin)
-    large::k_spec_sum<true><<<grid, 256, 0, s>>>(img, L, q, ldq, n, escale, wdot, ld, status);
+  if (outflag)
+    large::k_spec_sum<true><<<grid, 256, 0, s>>>(img, L, q, ldq, n, escale, outflag, wdot, ld,
+                                                 status);
   else
-    large::k_spec_sum<false><<<grid, 256, 0, s>>>(img, L, q, ldq, n, escale, wdot, ld, status);
+    large::k_spec_sum<false><<<grid, 256, 0, s>>>(img, L, q, ldq, n, escale, nullptr, wdot, ld,
+                                                  status);
   return cudaGetLastError();
 }
 
+// outflag: n words, cleared here before the pack.
 cudaError_t launch_pack_bf16(const double *q, int64_t ldq, int64_t n, int R, int Kh,
-                             const int *escale, void *A, int64_t lda, int sm_count,
-                             cudaStream_t s) {
+                             const int *escale, void *A, int64_t lda, unsigned *outflag,
+                             int sm_count, cudaStream_t s) {
   if (Kh % 64 || lda % 8) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(outflag, 0, (size_t)n * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
   const int64_t tiles = (n + 31) / 32 * (Kh / 64);
   const int grid = grid_for(tiles, 1, sm_count * 8);
   large::k_pack_bf16<<<grid, 256, 0, s>>>(q, ldq, n, R, Kh, escale,
-                                          static_cast<__nv_bfloat16 *>(A), lda);
+                                          static_cast<__nv_bfloat16 *>(A), lda, outflag);
   return cudaGetLastError();
 }
 
