@@ -19,7 +19,8 @@ ERRORS = {1: "bad argument", 2: "bad mechanism tables", 3: "CUDA error",
           4: "unsupported", 5: "timeout", 6: "no mechanism bound"}
 
 MODES = {"fp64": 0, "fp64_strict": 1, "mixed": 2, "fp64_tps": 3, "mixed_tps": 4,
-         "fp64_warp": 5, "mixed_warp": 6, "gemm": 7, "mixed_tile": 8}
+         "fp64_warp": 5, "mixed_warp": 6, "gemm": 7, "mixed_tile": 8,
+         "fp64_tile": 9}
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64

@@ -48,6 +48,9 @@ size_t large_rates_smem(const ImgLayout &L);
 cudaError_t launch_rates_tile(const unsigned char *img, const ImgLayout &L, const Batch &b,
                               int sm_count, int smem_optin, cudaStream_t s, double *q,
                               int64_t ldq, int *escale);
+cudaError_t launch_rates_tile64(const unsigned char *img, const ImgLayout &L, const Batch &b,
+                                int sm_count, int smem_optin, cudaStream_t s, double *q,
+                                int64_t ldq);
 cudaError_t launch_spec_sum(const unsigned char *img, const ImgLayout &L, const double *q,
                             int64_t ldq, int64_t n, const int *escale, const unsigned *outflag,
                             double *wdot, int64_t ld, int32_t *status, int sm_count,
@@ -573,11 +576,17 @@ int ws_end(crs_mech *m, cudaStream_t s) {
   return e == cudaSuccess ? CRS_OK : cuda_fail(e, "workspace ordering");
 }
 
-// Mixed precision in two passes (large mechanisms): per chunk, the
-// state-tile rates kernel writes the FP64 net rates, the species sums read
-// them.
-int wdot_two_pass(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
-  if ((size_t)crs::large_rates_smem(m->L) > (size_t)m->smem_optin)
+// Shared memory of a rates tile: FP32 (mixed) or FP64 concentrations of
+// 32 states.
+size_t tile_smem(const crs::ImgLayout &L, bool fp64) {
+  return fp64 ? (size_t)L.N * 32 * sizeof(double) : crs::large_rates_smem(L);
+}
+
+// Two passes (large mechanisms): per chunk, the state-tile rates kernel
+// (mixed precision, or FP64 throughout) writes the FP64 net rates, the
+// species sums read them.
+int wdot_two_pass(crs_mech *m, const crs::Batch &b, cudaStream_t s, bool fp64) {
+  if (tile_smem(m->L, fp64) > (size_t)m->smem_optin)
     return fail(CRS_ERR_UNSUPPORTED, "mechanism too large for the rates tile");
   std::lock_guard<std::mutex> lk(m->ws_mu);
   const int64_t rows = q_chunk(m->L, b.n);
@@ -591,8 +600,11 @@ int wdot_two_pass(crs_mech *m, const crs::Batch &b, cudaStream_t s) {
     bc.T = b.T + c0;
     bc.P = b.P + c0;
     bc.Y = b.Y + c0;
-    cudaError_t e = crs::launch_rates_tile(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
-                                           m->d_q, rows, nullptr);
+    cudaError_t e =
+        fp64 ? crs::launch_rates_tile64(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
+                                        m->d_q, rows)
+             : crs::launch_rates_tile(m->d_img, m->L, bc, m->sm_count, m->smem_optin, s,
+                                      m->d_q, rows, nullptr);
     if (e == cudaSuccess)
       e = crs::launch_spec_sum(m->d_img, m->L, m->d_q, rows, cnt, nullptr, nullptr,
                                b.wdot + c0, b.ld, m->d_status, m->sm_count, s);
@@ -656,26 +668,33 @@ int launch_mode(const crs_mech *m, crs::Batch &b, int mode, cudaStream_t s) {
       e = crs::launch_wdot_strict(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;
     case CRS_MODE_FP64:
-      // one state per thread when its columns fit on chip, else per warp
+      // one state per thread when its columns fit on chip; else the
+      // two-pass state-tile path (per warp when intermediates are asked for)
       e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
-      if (e == cudaErrorNotSupported)
+      if (e == cudaErrorNotSupported) {
+        if (!(b.conc || b.fwd || b.rev || b.pm) && tile_smem(m->L, true) <= (size_t)m->smem_optin)
+          return wdot_two_pass(const_cast<crs_mech *>(m), b, s, true);
         e = crs::launch_wdot_fp64(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
+      }
       break;
+    case CRS_MODE_FP64_TILE:
+      if (b.conc || b.fwd || b.rev || b.pm)
+        return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_FP64_TILE does not write intermediates");
+      return wdot_two_pass(const_cast<crs_mech *>(m), b, s, true);
     case CRS_MODE_MIXED:
       // one state per thread when its columns fit on chip; else the
       // two-pass state-tile path (per warp when intermediates are asked for)
       e = crs::launch_wdot_mixed_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       if (e == cudaErrorNotSupported) {
-        if (!(b.conc || b.fwd || b.rev || b.pm) &&
-            crs::large_rates_smem(m->L) <= (size_t)m->smem_optin)
-          return wdot_two_pass(const_cast<crs_mech *>(m), b, s);
+        if (!(b.conc || b.fwd || b.rev || b.pm) && tile_smem(m->L, false) <= (size_t)m->smem_optin)
+          return wdot_two_pass(const_cast<crs_mech *>(m), b, s, false);
         e = crs::launch_wdot_mixed(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       }
       break;
     case CRS_MODE_MIXED_TILE:
       if (b.conc || b.fwd || b.rev || b.pm)
         return fail(CRS_ERR_UNSUPPORTED, "CRS_MODE_MIXED_TILE does not write intermediates");
-      return wdot_two_pass(const_cast<crs_mech *>(m), b, s);
+      return wdot_two_pass(const_cast<crs_mech *>(m), b, s, false);
     case CRS_MODE_FP64_TPS:
       e = crs::launch_wdot_fp64_tps(m->d_img, m->L, b, m->sm_count, m->smem_optin, s);
       break;

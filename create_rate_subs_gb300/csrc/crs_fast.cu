@@ -28,6 +28,7 @@
 #include "crs_exp.cuh"
 #include "crs_internal.cuh"
 #include "crs_shapes.cuh"
+#include "crs_tile.cuh"
 
 namespace crs {
 
@@ -464,11 +465,28 @@ __device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
 // Four reactions of one shape (crs_shapes.cuh): rate constants, products
 // and net rates with compile-time trip counts, so that the four dependency
 // chains interleave; then their wdot contributions in order.
-template <int NR, int NP, int NNU, int REV, bool STAGES, class KC>
+// Sink of the on-chip kernels: net rates accumulate into the state's wdot
+// column, block by block or one reaction at a time, in order.
+struct WSink {
+  Col W;
+  template <int NNU>
+  __device__ __forceinline__ void block(const Tab &t, const int *rr, int cnt,
+                                        const double (&net)[4]) const {
+    accumulate<NNU>(t, rr, cnt, net, W);
+  }
+  __device__ __forceinline__ void one(const Tab &t, int r, double net) const {
+    for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
+      const int k = t.nu_sp[e];
+      W[k] = fma(t.nu_val[e], net, W[k]);
+    }
+  }
+};
+
+template <int NR, int NP, int NNU, int REV, bool STAGES, class KC, class CC, class SINK>
 __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
                                             int cnt, const State &s,
-                                            const Col &C, const KC &kc,
-                                            const Col &W, const Batch &b,
+                                            const CC &C, const KC &kc,
+                                            const SINK &sink, const Batch &b,
                                             int64_t i) {
   double net[4], x[4], e[4];
 #pragma unroll
@@ -520,41 +538,36 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
       if (REV && b.rev) b.rev[(int64_t)t.rev_idx[rr[u]] * b.ld + i] = rev[u];
     }
   }
-  accumulate<NNU>(t, rr, cnt, net, W);
+  sink.template block<NNU>(t, rr, cnt, net);
 }
 
-template <int SH, bool STAGES, class KC>
-__device__ __forceinline__ void run_shape(const Tab &t, const State &s,
-                                          const Col &C, const KC &S,
-                                          const Col &W, const Batch &b,
-                                          int64_t i) {
-  constexpr Shape d = shape_of(SH);
-  const int p0 = t.seg[SH], p1 = t.seg[SH + 1];
-  for (int p = p0; p < p1; p += 4) {
-    const int cnt = p1 - p < 4 ? p1 - p : 4;
-    int rr[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) rr[u] = t.perm[p + (u < cnt ? u : cnt - 1)];
-    shape_block<d.nr, d.np, d.nnu, d.rev, STAGES>(t, rr, cnt, s, C, S, W, b, i);
-  }
-}
-
-template <int SH, bool STAGES, class KC>
+// The shape groups' blocks of four reactions, in order; a caller that
+// splits the blocks among npart workers evaluates blocks part, part +
+// npart, ... of every group.
+template <int SH, bool STAGES, class KC, class CC, class SINK>
 struct Shapes {
   __device__ __forceinline__ static void run(const Tab &t, const State &s,
-                                             const Col &C, const KC &S,
-                                             const Col &W, const Batch &b,
-                                             int64_t i) {
-    run_shape<SH, STAGES>(t, s, C, S, W, b, i);
-    Shapes<SH + 1, STAGES, KC>::run(t, s, C, S, W, b, i);
+                                             const CC &C, const KC &S,
+                                             const SINK &sink, const Batch &b,
+                                             int64_t i, int part = 0, int npart = 1) {
+    constexpr Shape d = shape_of(SH);
+    const int p0 = t.seg[SH], p1 = t.seg[SH + 1];
+    for (int p = p0 + 4 * part; p < p1; p += 4 * npart) {
+      const int cnt = p1 - p < 4 ? p1 - p : 4;
+      int rr[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) rr[u] = t.perm[p + (u < cnt ? u : cnt - 1)];
+      shape_block<d.nr, d.np, d.nnu, d.rev, STAGES>(t, rr, cnt, s, C, S, sink, b, i);
+    }
+    Shapes<SH + 1, STAGES, KC, CC, SINK>::run(t, s, C, S, sink, b, i, part, npart);
   }
 };
-template <bool STAGES, class KC>
-struct Shapes<NSHAPE, STAGES, KC> {
+template <bool STAGES, class KC, class CC, class SINK>
+struct Shapes<NSHAPE, STAGES, KC, CC, SINK> {
   __device__ __forceinline__ static void run(const Tab &, const State &,
-                                             const Col &, const KC &,
-                                             const Col &, const Batch &,
-                                             int64_t) {}
+                                             const CC &, const KC &,
+                                             const SINK &, const Batch &,
+                                             int64_t, int = 0, int = 1) {}
 };
 
 // Net rate (fwd - rev) * pres_mod of any reaction: general rate forms,
@@ -585,10 +598,10 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   return net;
 }
 
-template <bool STAGES, class KC>
+template <bool STAGES, class KC, class CC, class SINK>
 __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
-                                        double mix, const Col &C,
-                                        const KC &S, const Col &W,
+                                        double mix, const CC &C,
+                                        const KC &S, const SINK &sink,
                                         const Batch &b, int64_t i) {
   double fwd, rev, pm;
   const double net = rxn_net(t, r, s, mix, C, S, fwd, rev, pm);
@@ -598,10 +611,7 @@ __device__ __forceinline__ void general(const Tab &t, int r, const State &s,
     if (b.rev && j >= 0) b.rev[(int64_t)j * b.ld + i] = rev;
     if (b.pm && p >= 0) b.pm[(int64_t)p * b.ld + i] = pm;
   }
-  for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
-    const int k = t.nu_sp[e];
-    W[k] = fma(t.nu_val[e], net, W[k]);
-  }
+  sink.one(t, r, net);
 }
 
 // KCM 0: Kc from a per-species Gibbs column S (3 columns of 8 B per
@@ -675,11 +685,12 @@ __global__ void __launch_bounds__(256, 1)
     if (STAGES && b.conc)
       for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = C[k];
     const double mix = P * s.invT * INV_RU;
+    const WSink sink{W};
     if constexpr (KCM == 0) {
       const KcCol<Col> kc{S};
-      Shapes<0, STAGES, KcCol<Col>>::run(t, s, C, kc, W, b, i);
+      Shapes<0, STAGES, KcCol<Col>, Col, WSink>::run(t, s, C, kc, sink, b, i);
       for (int p = t.seg[NSHAPE]; p < t.R; ++p)
-        general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
+        general<STAGES>(t, t.perm[p], s, mix, C, kc, sink, b, i);
     } else {
       using KC = typename std::conditional<KCM == 1, KcPoly1, KcPolyG>::type;
       KC kc;
@@ -687,9 +698,9 @@ __global__ void __launch_bounds__(256, 1)
       kc.logT = s.logT;
       kc.invT = s.invT;
       if constexpr (KCM == 1) kc.Tbits = Tbits;
-      Shapes<0, STAGES, KC>::run(t, s, C, kc, W, b, i);
+      Shapes<0, STAGES, KC, Col, WSink>::run(t, s, C, kc, sink, b, i);
       for (int p = t.seg[NSHAPE]; p < t.R; ++p)
-        general<STAGES>(t, t.perm[p], s, mix, C, kc, W, b, i);
+        general<STAGES>(t, t.perm[p], s, mix, C, kc, sink, b, i);
     }
     for (int k = 0; k < N; ++k) {
       const double v = W[k];
@@ -699,6 +710,74 @@ __global__ void __launch_bounds__(256, 1)
   }
   if (bad && b.status) atomicAdd(&b.status[1], bad);
   sched_done(b.sched, amask, lane);
+}
+
+// ---- state tiles (two passes over HBM; see crs_large.cu) ---------------
+// FP64 concentrations of a tile of 32 states in shared memory ([N][32],
+// 256 B per species), FTW warps taking the shape blocks round-robin, every
+// net rate written to HBM for the species sums.  For mechanisms whose
+// per-thread columns do not fit on chip.
+constexpr int FTW = 8;
+
+template <bool KC1>
+__global__ void __launch_bounds__(FTW * 32, 1)
+    k_rates_tile64(const unsigned char *__restrict__ img, ImgLayout L, Batch b,
+                   tile::RatesOut o) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ double s_rho[32], s_yN[32];
+  __shared__ int64_t s_tile;
+  const Tab t = make_tab(img, L);
+  const int N = t.N, R = t.R;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Col C{reinterpret_cast<double *>(smem) + lane, 32};
+  const int64_t ntiles = (b.n + 31) / 32;
+  for (;;) {
+    const int64_t tile = tile::next_tile(b.sched, &s_tile);
+    if (tile >= ntiles) break;
+    const int64_t i = tile * 32 + lane;
+    const bool valid = i < b.n;
+    const int64_t ic = valid ? i : tile * 32;  // idle lanes repeat a valid state
+    State s;
+    s.T = b.T[ic];
+    const double P = b.P[ic];
+    s.P = P;
+    s.invT = 1.0 / s.T;
+    s.logT = log(s.T);
+    s.tab = t.exptab;
+    if (warp == 0) {
+      // y_N = 1 - sum y in the reference's left-to-right order
+      // (rate_subs.py:1312-1320), and the mean molecular weight
+      double ys = N > 1 ? b.Y[ic] : 0.0, mwi = 0.0;
+      for (int k = 1; k < N - 1; ++k) ys += b.Y[(int64_t)k * b.ld + ic];
+      const double yN = 1.0 - ys;
+      for (int k = 0; k < N - 1; ++k) mwi = fma(b.Y[(int64_t)k * b.ld + ic], t.inv_mw[k], mwi);
+      mwi = fma(yN, t.inv_mw[N - 1], mwi);
+      s_rho[lane] = P / mwi * (s.invT * INV_RU);
+      s_yN[lane] = yN;
+    }
+    __syncthreads();
+    const double rho = s_rho[lane];
+    for (int k = warp; k < N; k += FTW) {
+      const double y = k == N - 1 ? s_yN[lane] : b.Y[(int64_t)k * b.ld + ic];
+      C[k] = y * (rho * t.inv_mw[k]);
+    }
+    __syncthreads();
+    const double mix = P * s.invT * INV_RU;
+    using KC = typename std::conditional<KC1, KcPoly1, KcPolyG>::type;
+    KC kc;
+    kc.T = s.T;
+    kc.logT = s.logT;
+    kc.invT = s.invT;
+    if constexpr (KC1) kc.Tbits = __double_as_longlong(s.T);
+    int esum = 0, ecnt = 0;
+    const tile::QSink sink{o.q + i, o.ldq, valid, esum, ecnt};
+    Shapes<0, false, KC, Col, tile::QSink>::run(t, s, C, kc, sink, b, i, warp, FTW);
+    for (int p = t.seg[NSHAPE] + warp; p < R; p += FTW)
+      general<false>(t, t.perm[p], s, mix, C, kc, sink, b, i);
+    // the next tile replaces C only after every warp is done with this one
+    __syncthreads();
+  }
+  tile::tiles_done(b.sched);
 }
 
 // ---- warp per state -----------------------------------------------------
@@ -849,6 +928,25 @@ cudaError_t launch_wdot_fp64_tps(const unsigned char *img, const ImgLayout &L,
   const cudaError_t e = set_smem_limit(k, bytes);
   if (e != cudaSuccess) return e;
   k<<<grid_for(b.n, block, sm_count), block, bytes, s>>>(img, L, b);
+  return cudaGetLastError();
+}
+
+// FP64 rates of n states (b: chunk-local, no intermediates) into q [R][ldq]
+// by state tiles; b.sched must be a free counter pair.
+cudaError_t launch_rates_tile64(const unsigned char *img, const ImgLayout &L, const Batch &b,
+                                int sm_count, int smem_optin, cudaStream_t s, double *q,
+                                int64_t ldq) {
+  const size_t bytes = (size_t)L.N * 32 * sizeof(double);
+  if (bytes > (size_t)smem_optin || !b.sched) return cudaErrorNotSupported;
+  auto k = L.kc_single ? fast::k_rates_tile64<true> : fast::k_rates_tile64<false>;
+  cudaError_t e = set_smem_limit(k, bytes);
+  if (e != cudaSuccess) return e;
+  int per_sm = 1;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, fast::FTW * 32, bytes);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorNotSupported;
+  const int grid = grid_for((b.n + 31) / 32, 1, sm_count * per_sm);
+  k<<<grid, fast::FTW * 32, bytes, s>>>(img, L, b, tile::RatesOut{q, ldq, nullptr});
   return cudaGetLastError();
 }
 

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "crs_mixed.cuh"
+#include "crs_tile.cuh"
 
 namespace crs {
 namespace large {
@@ -41,38 +42,8 @@ using namespace mixed;
 constexpr int TW = 4;        // warps per CTA of the rates kernel
 constexpr int WINDOW = 100;  // binary orders around c_s carried by bf16 hi + lo
 
-// Per-chunk outputs of the rates kernel.
-struct RatesOut {
-  double *q;      // [R][ldq]: net rate of reaction r for chunk state i
-  int64_t ldq;
-  int *escale;    // [n]: scale exponent c_i (mean binary exponent of the nonzero rates)
-};
-
-// Sink of the rates kernel: the lane's net rates to HBM, and the running
-// sum / count of their binary exponents (integer work on the bit pattern).
-struct QSink {
-  double *q;  // this lane's column
-  int64_t ldq;
-  bool valid;
-  int &esum, &ecnt;
-  __device__ __forceinline__ void put(int r, double v) const {
-    if (valid) q[(int64_t)r * ldq] = v;
-    const int hi = __double2hiint(v);
-    const int e = (hi >> 20) & 0x7ff;
-    if (e != 0x7ff && ((hi & 0x7fffffff) | __double2loint(v)) != 0) {
-      esum += e - 1023;
-      ++ecnt;
-    }
-  }
-  template <int NNU>
-  __device__ __forceinline__ void block(const Tab &, const int *rr, int cnt,
-                                        const double (&net)[4]) const {
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (u < cnt) put(rr[u], net[u]);
-  }
-  __device__ __forceinline__ void one(const Tab &, int r, double net) const { put(r, net); }
-};
+using tile::QSink;
+using tile::RatesOut;
 
 template <bool KC1>
 __global__ void __launch_bounds__(TW * 32, 3)
@@ -88,9 +59,7 @@ __global__ void __launch_bounds__(TW * 32, 3)
   const FCol C{Cs + lane, 32};
   const int64_t ntiles = (b.n + 31) / 32;
   for (;;) {
-    if (threadIdx.x == 0) s_tile = (int64_t)atomicAdd(b.sched, 1ULL);
-    __syncthreads();
-    const int64_t tile = s_tile;
+    const int64_t tile = tile::next_tile(b.sched, &s_tile);
     if (tile >= ntiles) break;
     const int64_t i = tile * 32 + lane;
     const bool valid = i < b.n;
@@ -147,27 +116,13 @@ __global__ void __launch_bounds__(TW * 32, 3)
         es += s_es[w][lane];
         ec += s_ec[w][lane];
       }
-      // nearest integer to es / ec by integer arithmetic
-      int c = 0;
-      if (ec) {
-        const int a = es >= 0 ? es : -es;
-        c = (2 * a + ec) / (2 * ec);
-        if (es < 0) c = -c;
-      }
-      o.escale[i] = c;
+      o.escale[i] = tile::scale_exponent(es, ec);
     }
     // the next tile replaces C and the tile number only after every warp
     // is done with this one
     __syncthreads();
   }
-  // the launch's last CTA puts the tile counter back for the next launch
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(b.sched + 1, 1ULL) == (unsigned long long)gridDim.x - 1) {
-      atomicExch(b.sched, 0ULL);
-      atomicExch(b.sched + 1, 0ULL);
-    }
-  }
+  tile::tiles_done(b.sched);
 }
 
 __device__ __forceinline__ bool in_window(double v, int c) {
@@ -303,7 +258,7 @@ cudaError_t launch_rates_tile(const unsigned char *img, const ImgLayout &L, cons
   if (per_sm < 1) return cudaErrorNotSupported;
   const int64_t ntiles = (b.n + 31) / 32;
   const int grid = grid_for(ntiles, 1, sm_count * per_sm);
-  k<<<grid, large::TW * 32, bytes, s>>>(img, L, b, large::RatesOut{q, ldq, escale});
+  k<<<grid, large::TW * 32, bytes, s>>>(img, L, b, tile::RatesOut{q, ldq, escale});
   return cudaGetLastError();
 }
 

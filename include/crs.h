@@ -72,11 +72,16 @@ typedef struct crs_mech crs_mech;
  * sums.  CRS_MODE_MIXED takes this path when a mechanism's per-thread
  * columns do not fit on chip and no intermediates are asked for.  No
  * intermediates.
- * CRS_MODE_GEMM and the two-pass path use a workspace owned by the handle,
+ * CRS_MODE_GEMM and the two-pass paths use a workspace owned by the handle,
  * allocated on first use (FP64 rates of up to 2^17 states, <= ~2 GiB, plus
  * 4 bytes per reaction and state for the contraction): calls on one handle
  * take turns on the GPU, whatever their streams. */
 #define CRS_MODE_MIXED_TILE 8
+/* The arithmetic of CRS_MODE_FP64 in the same two passes (FP64
+ * concentrations of the tile in shared memory); CRS_MODE_FP64 takes this
+ * path when the per-thread columns do not fit and no intermediates are
+ * asked for. */
+#define CRS_MODE_FP64_TILE 9
 
 /* ---- mechanism tables ------------------------------------------------ */
 

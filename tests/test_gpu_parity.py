@@ -278,7 +278,8 @@ def test_large_mechanism_all_modes(synth_mech):
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-@pytest.mark.parametrize("mode,tol", [("mixed_tile", TOL_WDOT_MIXED), ("gemm", 1e-4)])
+@pytest.mark.parametrize("mode,tol", [("mixed_tile", TOL_WDOT_MIXED), ("gemm", 1e-4),
+                                      ("fp64_tile", TOL_WDOT_FP64)])
 def test_two_pass_modes_vs_golden(case, mode, tol, golden):
     """The two-pass state-tile path (FP64 net rates through HBM, then the
     species sums or the tensor-core contraction) against the reference's
@@ -313,7 +314,8 @@ def test_two_pass_matches_oracle_odd_sizes(name, synth_mech):
         lib = _lib.load()
         p = lambda t: ctypes.c_void_p(t.data_ptr())
         st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        for mode, tol in (("mixed_tile", TOL_WDOT_MIXED), ("gemm", 1e-4)):
+        for mode, tol in (("mixed_tile", TOL_WDOT_MIXED), ("gemm", 1e-4),
+                          ("fp64_tile", TOL_WDOT_FP64)):
             W = torch.full((N, ld), 7.0, dtype=torch.float64, device="cuda")
             _lib.check(lib.crs_wdot(rs.h, n, p(dT), p(dP), p(dY), ld, p(W), _lib.MODES[mode],
                                     st))
