@@ -67,11 +67,21 @@ def _args():
     return ap.parse_args()
 
 
-def _mechanism():
+def _mechanism(name=MECH):
+    """The synthetic mechanism ``name``.  Where the reference's emitted C of
+    it is built (oracle/_ref/<name>/), its Chemkin text is the one that build
+    was generated from (oracle/_ref/<name>/_mech/), so that the accuracy
+    check and the reference arm see the same mechanism as the timed kernels;
+    the generator's least-squares thermo fits can differ in a printed digit
+    between hosts."""
     from create_rate_subs_gb300 import synth
     from create_rate_subs_gb300.mechanism import Mechanism
-    d = tempfile.mkdtemp(prefix="crs_bench_")
-    mp, tp = synth.write_mechanism(MECH, d)
+    mdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle",
+                        "_ref", name, "_mech")
+    mp = os.path.join(mdir, name + ".inp")
+    tp = os.path.join(mdir, name + "_therm.dat")
+    if not (os.path.exists(mp) and os.path.exists(tp)):
+        mp, tp = synth.write_mechanism(name, tempfile.mkdtemp(prefix="crs_bench_"))
     return Mechanism.from_chemkin(mp, tp)
 
 
@@ -674,9 +684,7 @@ def _bench_large(args, stream, dist, world, peaks, rank):
     from create_rate_subs_gb300 import _lib, synth
     from create_rate_subs_gb300.mechanism import Mechanism
     from create_rate_subs_gb300.rates import RateSubs
-    d = tempfile.mkdtemp(prefix="crs_bench_large_")
-    mp, tp = synth.write_mechanism("large561", d)
-    mech = Mechanism.from_chemkin(mp, tp)
+    mech = _mechanism("large561")
     rs = RateSubs(mech)
     N = mech.n_species
     n = args.large_states
@@ -768,8 +776,7 @@ def run_profile_large(args):
     from create_rate_subs_gb300.mechanism import Mechanism
     from create_rate_subs_gb300.rates import RateSubs
     torch.cuda.set_device(0)
-    d = tempfile.mkdtemp(prefix="crs_prof_large_")
-    mech = Mechanism.from_chemkin(*synth.write_mechanism("large561", d))
+    mech = _mechanism("large561")
     rs = RateSubs(mech)
     n = 1 << 16
     T, P, Y = synth.make_states(mech.n_species, n, seed=5)

@@ -12,7 +12,9 @@ Recipe, two steps:
     ``create_rate_subs('c', mech, therm)`` in a scratch working directory
     and copies the emitted ``chem_utils.c``, ``rxn_rates.c``,
     ``rxn_rates_pres_mod.c``, ``spec_rates.c``, ``dydt.c`` and their headers into
-    ``oracle/_ref/<name>/``.  Nothing is written to the reference checkout.
+    ``oracle/_ref/<name>/``, with the mechanism text they were emitted from
+    in ``oracle/_ref/<name>/_mech/`` (``mechanism_files``).  Nothing is
+    written to the reference checkout.
 
 ``compile``  (needs only ``oracle/_ref/<name>/`` and ``oracle/ref_harness.c``)
     Compiles the emitted files with the batch driver into
@@ -104,7 +106,32 @@ def generate(name, mech_path, therm_path, reference=None, last_spec=None):
                 shutil.copy(p, dst)
         with open(os.path.join(dst, "generator.log"), "w") as f:
             f.write(res.stdout + res.stderr)
+        # the mechanism text the C was emitted from: tests and the bench
+        # parse this same text, so that they compare functions of one input
+        mdir = os.path.join(dst, "_mech")
+        os.makedirs(mdir)
+        shutil.copy(mech_path, mdir)
+        if therm_path:
+            shutil.copy(therm_path, mdir)
     return dst
+
+
+def mechanism_files(name):
+    """(mech_path, therm_path) of the text the emitted C of ``name`` was
+    generated from, or None when that build is absent.
+
+    The synthetic generator fits NASA-7 polynomials with LAPACK least
+    squares, whose last bits differ between BLAS builds (x86 and Arm), and a
+    coefficient printed with nine digits can then round the other way: a text
+    regenerated on another host may differ from the one the reference's C
+    encodes.  Comparisons against ``RefLib(name)`` therefore parse this
+    file."""
+    mdir = os.path.join(ref_dir(name), "_mech")
+    mp = os.path.join(mdir, name + ".inp")
+    tp = os.path.join(mdir, name + "_therm.dat")
+    if os.path.exists(mp) and os.path.exists(tp):
+        return mp, tp
+    return None
 
 
 def _max_index(text, array):
@@ -194,13 +221,9 @@ def main(argv):
     from create_rate_subs_gb300 import synth
     for name in argv[2:]:
         if argv[1] in ("generate", "all"):
-            mdir = os.path.join(REF_OUT, name, "_mech")
             tmpdir = tempfile.mkdtemp(prefix="crs_mech_")
             mp, tp = synth.write_mechanism(name, tmpdir)
             generate(name, mp, tp)
-            os.makedirs(mdir, exist_ok=True)
-            shutil.copy(mp, mdir)
-            shutil.copy(tp, mdir)
             shutil.rmtree(tmpdir)
         if argv[1] in ("compile", "all"):
             print(compile_ref(name))

@@ -46,16 +46,23 @@ def golden():
 
 @pytest.fixture(scope="session")
 def synth_mech():
-    """Mechanism objects of the synthetic workloads, by name."""
+    """Mechanism objects of the synthetic workloads, by name.  Where the
+    reference's emitted C of a workload is built, the mechanism is parsed
+    from the text that C was generated from (oracle.build_ref.
+    mechanism_files), so that comparisons with RefLib see one mechanism on
+    every host."""
     from create_rate_subs_gb300 import synth
     from create_rate_subs_gb300.mechanism import Mechanism
+    from oracle import build_ref
     cache = {}
 
     def get(name):
         if name not in cache:
-            d = tempfile.mkdtemp(prefix="crs_mech_")
-            mp, tp = synth.write_mechanism(name, d)
-            cache[name] = Mechanism.from_chemkin(mp, tp)
+            files = build_ref.mechanism_files(name)
+            if files is None:
+                d = tempfile.mkdtemp(prefix="crs_mech_")
+                files = synth.write_mechanism(name, d)
+            cache[name] = Mechanism.from_chemkin(*files)
         return cache[name]
     return get
 

@@ -36,6 +36,21 @@ def test_oracle_bitexact_vs_reference_build(name, n, synth_mech):
         assert np.array_equal(a[k], b[k]), k
 
 
+@pytest.mark.parametrize("name", ["small", "gri53", "large561"])
+def test_reference_build_keeps_its_mechanism_text(name):
+    """The reference build of each workload keeps the Chemkin text it was
+    emitted from, and on this host the generator still writes that text."""
+    import tempfile
+    from oracle import build_ref
+    files = build_ref.mechanism_files(name)
+    if files is None:
+        pytest.skip("reference C not built here (python oracle/build_ref.py all %s)" % name)
+    fresh = synth.write_mechanism(name, tempfile.mkdtemp(prefix="crs_mech_"))
+    for a, b in zip(files, fresh):
+        with open(a) as fa, open(b) as fb:
+            assert fa.read() == fb.read(), a
+
+
 def test_oracle_omp_matches_serial(golden):
     mech, g = golden("gri53")
     o = Oracle(mech.blob)
