@@ -791,8 +791,11 @@ def run_profile_large(args):
 
 
 def run_profile_surrogate(args):
-    """Features, the four layer GEMMs and the output kernel of the surrogate
-    network (random weights) over 2^20 states, once."""
+    """The surrogate network (random weights) over 2^20 states, once each:
+    the gated inference path (k_features, the one-kernel network
+    k_mlp_infer, k_output), then the layer-by-layer forward pass that
+    training uses (four k_gemm launches with fused bias+SiLU epilogues) on
+    the same features."""
     import torch
     from create_rate_subs_gb300.rates import RateSubs
     from create_rate_subs_gb300.surrogate import Surrogate
@@ -801,10 +804,15 @@ def run_profile_surrogate(args):
     sur = Surrogate(rs, seed=0)
     n = 1 << 20
     T, P, Y = sur.sample_states(n, seed=5)
-    w, nfb = sur.wdot(T, P, Y[: rs.n_species - 1].contiguous(), tol=float("inf"),
-                      with_fallback=False)
+    Y = Y[: rs.n_species - 1].contiguous()
+    w, nfb = sur.wdot(T, P, Y, tol=float("inf"), with_fallback=False)
+    X = torch.zeros((n, sur.net.pad[0]), dtype=torch.bfloat16, device="cuda")
+    sur.features(T, P, Y, Y.stride(0), n, X, box=False)
+    Yh = torch.empty((n, sur.net.pad[-1]), dtype=torch.float32, device="cuda")
+    sur.net.forward(X, n, Yh)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "surrogate network, %d states, one pass" % n}))
+    print(json.dumps({"profile_case": "surrogate network, %d states: gated inference, "
+                      "then the layer-by-layer forward" % n}))
     return 0
 
 

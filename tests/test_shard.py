@@ -59,3 +59,65 @@ def test_two_gloo_ranks_cover_the_batch():
         assert p.exitcode == 0
     assert count == n
     assert total == float(np.sum(np.arange(n) * 3.0 + 1.0))
+
+
+def _wdot_worker(rank, world, port, out):
+    """One rank: its slab of the golden 53-species states through the
+    reference's per-state functions on the host (crs_state_* on a host-only
+    handle), then a sum over ranks of the (species, states) array in which
+    each rank filled only its own columns (x + 0 is exact)."""
+    import ctypes
+    from conftest import load_golden
+    from create_rate_subs_gb300 import _lib
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mech, g = load_golden("gri53")
+    N, R, NREV, NPM = (int(x) for x in g["dims"])
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    _lib.check(lib.crs_mech_load_host(mech.blob, len(mech.blob), ctypes.byref(h)))
+    dp = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    n = g["T"].shape[0]
+    a, b = shard_range(n, rank, world)
+    full = torch.zeros((N, n), dtype=torch.float64)
+    conc, fwd = np.zeros(N), np.zeros(R)
+    rev, pm = np.zeros(max(NREV, 1)), np.zeros(max(NPM, 1))
+    sp, dyN = np.zeros(N - 1), ctypes.c_double()
+    yN, mw, rho = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    for i in range(a, b):
+        T, P = float(g["T"][i]), float(g["P"][i])
+        y = np.ascontiguousarray(g["Y"][: N - 1, i])
+        _lib.check(lib.crs_state_eval_conc(h, T, P, dp(y), ctypes.byref(yN), ctypes.byref(mw),
+                                           ctypes.byref(rho), dp(conc)))
+        _lib.check(lib.crs_state_eval_rxn_rates(h, T, P, dp(conc), dp(fwd), dp(rev)))
+        _lib.check(lib.crs_state_get_rxn_pres_mod(h, T, P, dp(conc), dp(pm)))
+        _lib.check(lib.crs_state_eval_spec_rates(h, dp(fwd), dp(rev), dp(pm), dp(sp),
+                                                 ctypes.byref(dyN)))
+        full[: N - 1, i] = torch.from_numpy(sp)
+        full[N - 1, i] = dyN.value
+    lib.crs_mech_free(h)
+    dist.all_reduce(full)
+    if rank == 0:
+        out.put((b - a, bool(np.array_equal(full.numpy(), g["wdot"]))))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_evaluate_their_slabs():
+    """Two gloo ranks each evaluate their slab of a batch with the host
+    per-state functions; the combined species rates equal the reference's
+    golden vectors bit for bit."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_wdot_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    slab0, exact = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert slab0 > 0
+    assert exact
