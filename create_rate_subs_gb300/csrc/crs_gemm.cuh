@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(NT, ST <= 2 ? 2 : 1)
 
   // split-K: grid z slice z covers K blocks [z * kblocks, (z + 1) * kblocks)
   const int kb0 = blockIdx.z * kblocks;
+  int issued = 0;  // K blocks whose TMA loads the producer lane started
   if (warp == 0 && lane == 0) {
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % ST;
@@ -154,6 +155,7 @@ __global__ void __launch_bounds__(NT, ST <= 2 ? 2 : 1)
       expect_tx(&full[s], A_BYTES + B_BYTES);
       tma_2d(sA + s * A_BYTES, &tmA, (kb0 + kb) * BK, m0, &full[s]);
       tma_2d(sB + s * B_BYTES, &tmB, (kb0 + kb) * BK, n0, &full[s]);
+      ++issued;
     }
   } else if (warp == 1 && lane == 0) {
     const uint32_t id = idesc<BN>();
@@ -190,7 +192,23 @@ __global__ void __launch_bounds__(NT, ST <= 2 ? 2 : 1)
     atomicOr(&status[0], STATUS_GEMM_TIMEOUT);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
+  const int gave_up = __syncthreads_or(failed || !got);
+  // A CTA that gave up must not free its TMEM while MMAs may still write it,
+  // nor leave while TMA loads may still write its shared memory: wait for
+  // both once more (bounded, 4x longer).  The latest load of each stage
+  // completes last, so its phase covers the stage's earlier loads.
+  if (gave_up) {
+    if (threadIdx.x == 0) {
+      for (int r = 0; r < 4 && !wait_bounded(&done, 0); ++r) {
+      }
+    }
+    if (warp == 0 && lane == 0) {
+      for (int kb = issued > ST ? issued - ST : 0; kb < issued; ++kb)
+        for (int r = 0; r < 4 && !wait_bounded(&full[kb % ST], (uint32_t)(kb / ST) & 1u); ++r) {
+        }
+    }
+    __syncthreads();
+  }
   if (warp == 2) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL)
