@@ -54,7 +54,14 @@ def _args():
     ap.add_argument("--sur-epochs", type=int, default=8)
     ap.add_argument("--sur-eval", type=int, default=1 << 24,
                     help="fresh states the surrogate is evaluated on")
-    ap.add_argument("--sur-tol", type=float, default=0.05)
+    ap.add_argument("--sur-bound", type=float, default=0.1,
+                    help="error bound the surrogate's gate is calibrated for")
+    ap.add_argument("--sur-gate-states", type=int, default=1 << 23,
+                    help="held-out states the error network is trained on")
+    ap.add_argument("--sur-cal-states", type=int, default=1 << 24,
+                    help="held-out states the gate threshold is calibrated on")
+    ap.add_argument("--sur-margin", type=float, default=0.5,
+                    help="calibrate for margin x bound on the held-out states")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--profile-surrogate", action="store_true",
                     help="one surrogate network forward pass over 2^20 states "
@@ -402,13 +409,13 @@ def run_ours(args):
     value = n * world / (ms * 1e-3)
     per_mode = {}
     for m in modes:
-        msm = _time_steps(lambda: rs.wdot(dT, dP, dY, m, out=out), max(2, args.steps // 2), 1,
+        msm = _time_steps(lambda: rs.wdot(dT, dP, dY, m, out=out), max(3, args.steps // 2), 3,
                           stream, dist)
         per_mode[m] = {"value": n * world / (msm * 1e-3), "ms_per_step": msm}
     strict = None
     if plain != "fp64_strict":
         ms_s = _time_steps(lambda: rs.wdot(dT, dP, dY, "fp64_strict", out=out),
-                           max(2, args.steps // 2), 1, stream, dist)
+                           max(3, args.steps // 2), 3, stream, dist)
         strict = {"value": n * world / (ms_s * 1e-3), "unit": "states/s",
                   "ms_per_step": ms_s,
                   "note": "FP64 in the reference's own operation order (CUDA exp/log/pow, "
@@ -431,7 +438,7 @@ def run_ours(args):
         msm = _time_steps(lambda: rs.wdot(mT, mP, mY, "mixed", out=mo), args.steps,
                           args.warmup, stream, dist)
         ms_plain22 = _time_steps(lambda: rs.wdot(mT, mP, mY, plain, out=mo),
-                                 max(2, args.steps // 2), 1, stream, dist)
+                                 max(3, args.steps // 2), 3, stream, dist)
         subm = 1 << 16
         err22 = _ref_accuracy(
             MECH, mech, T2[:subm], P2[:subm], Y2[:, :subm],
@@ -463,7 +470,7 @@ def run_ours(args):
             if m not in modes:
                 continue
             msd = _time_steps(lambda: rs.dydt(arg, ydy, conv=conv, mode=m, out=dyo),
-                              max(2, args.steps // 2), 1, stream, dist)
+                              max(3, args.steps // 2), 3, stream, dist)
             dydt_res["%s_%s" % (form, m)] = {"value": n * world / (msd * 1e-3),
                                              "unit": "states/s", "ms_per_step": msd}
     del ydy, dyo, rho
@@ -547,10 +554,12 @@ def run_ours(args):
 
 
 def _bench_surrogate(args, rs, stream, dist, world, rank):
-    """The learned surrogate on the 53-species mechanism: trained by the
-    library's own bf16 kernels on states labelled by the exact FP64 kernel,
-    evaluated with fallback on fresh states; error against the exact FP64
-    kernel on every evaluated state."""
+    """The learned surrogate on the 53-species mechanism: two networks
+    trained by the library's own bf16 kernels on states labelled by the
+    exact FP64 kernel, an error network trained on held-out labelled states,
+    the gate threshold calibrated for an error bound on further held-out
+    states, then evaluation with fallback on fresh states: states/s and the
+    error against the exact FP64 kernel on every evaluated state."""
     import torch
     from create_rate_subs_gb300.surrogate import Surrogate
     N = rs.n_species
@@ -559,7 +568,6 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     n_tr = (args.sur_train + B - 1) // B * B
     T, P, Y = sur.sample_states(n_tr, seed=5000 + rank)
     torch.cuda.synchronize()
-    t0 = time.time()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     losses = sur.fit(states=(T, P, Y), epochs=args.sur_epochs, lr=2e-3, lr_final=2e-5)
@@ -568,8 +576,22 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     fit_s = e0.elapsed_time(e1) * 1e-3
     del T, P, Y
     torch.cuda.empty_cache()
+    e0.record(stream)
+    gate_losses = sur.fit_gate(n=args.sur_gate_states, epochs=12, seed=6000 + rank)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gate_fit_s = e0.elapsed_time(e1) * 1e-3
+    # calibration: scores and errors of held-out states, thresholds per bound
+    Tc, Pc, Yc = sur.sample_states(args.sur_cal_states, seed=6500 + rank)
+    _, g_cal, e_cal = sur.gate_scores(Tc, Pc, Yc)
+    del Tc, Pc, Yc
+    torch.cuda.empty_cache()
+    bound, margin = args.sur_bound, args.sur_margin
+    stol = sur.threshold(g_cal, e_cal, margin * bound)
+    sur.stol, sur.bound = stol, bound
     net = sur.net
     macs = sum(net.dims[l] * net.dims[l + 1] for l in range(net.L))
+    emacs = sum(sur.err_net.dims[l] * sur.err_net.dims[l + 1] for l in range(sur.err_net.L))
     bwd_data = sum(net.dims[l] * net.dims[l + 1] for l in range(1, net.L))
     train_flops_state = 2 * (2 * macs + bwd_data)
     # a timed training pass alone (steps after the fit, same buffers)
@@ -586,26 +608,25 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     Ye = Ye[: N - 1].contiguous()
     out = torch.empty((N, ne), dtype=torch.float64, device="cuda")
     exact = torch.empty((N, ne), dtype=torch.float64, device="cuda")
-    tol = args.sur_tol
-    ms_sur = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tol, out=out), 3, 1, stream, dist)
-    ms_net = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tol, out=out, with_fallback=False),
-                         3, 1, stream, dist)
-    ms_plain = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "fp64", out=exact), 3, 1, stream, dist)
-    ms_mixed = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "mixed", out=exact), 3, 1, stream, dist)
-    # the network's layers alone (features already in X)
+    ms_sur = _time_steps(lambda: sur.wdot(Te, Pe, Ye, out=out), 3, 3, stream, dist)
+    ms_net = _time_steps(lambda: sur.wdot(Te, Pe, Ye, out=out, with_fallback=False),
+                         3, 3, stream, dist)
+    ms_plain = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "fp64", out=exact), 3, 3, stream, dist)
+    ms_mixed = _time_steps(lambda: rs.wdot(Te, Pe, Ye, "mixed", out=exact), 3, 3, stream, dist)
+    # one network's layers alone (features already in X)
     M = (ne + 127) // 128 * 128
     X = torch.zeros((M, net.pad[0]), dtype=torch.bfloat16, device="cuda")
     sur.features(Te, Pe, Ye, ne, ne, X, box=False)
     Yh = torch.empty((ne, net.pad[-1]), dtype=torch.float32, device="cuda")
-    ms_fwd = _time_steps(lambda: net.forward(X, ne, Yh), 5, 2, stream, dist)
-    ms_inf = _time_steps(lambda: net.infer(X, ne, Yh), 5, 2, stream, dist)
+    ms_fwd = _time_steps(lambda: net.forward(X, ne, Yh), 5, 3, stream, dist)
+    ms_inf = _time_steps(lambda: net.infer(X, ne, Yh), 5, 3, stream, dist)
     del X, Yh
-    # error of the gated result and of the raw network, on every state
+    # error of the gated result and of the served network result, every state
     rs.wdot(Te, Pe, Ye, "fp64", out=exact)
-    w, nfb = sur.wdot(Te, Pe, Ye, tol=tol, out=out)
-    raw = torch.empty_like(out)
-    sur.wdot(Te, Pe, Ye, tol=tol, out=raw, with_fallback=False)
-    den = exact.abs() + sur.scale[:, None]
+    w, nfb = sur.wdot(Te, Pe, Ye, out=out)
+    raw, flag, _ = sur._serve(Te, Pe, Ye, tol=0.05)
+    e_raw = sur.served_error(raw, exact)
+    served = flag == 0
 
     def q(e):
         if e.numel() == 0:
@@ -614,20 +635,19 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
         n_ = k.numel()
         return {"p50": float(k[n_ // 2]), "p90": float(k[int(n_ * 0.9)]),
                 "p99": float(k[int(n_ * 0.99)]), "max": float(k[-1])}
-    err_gated = q(((w - exact).abs() / den).amax(dim=0))
-    e_raw = ((raw - exact).abs() / den).amax(dim=0)
+    err_gated = q(sur.served_error(w, exact))
     err_raw = q(e_raw)
-    served = (w == raw).all(dim=0)          # states the network answered
     err_served = q(e_raw[served])
-    # the gate's trade-off: tighter residual tolerances send more states to
-    # the exact kernel
+    # the trade-off: other bounds, each threshold from the same calibration
     sweep = []
-    for tl in (0.05, 0.01, 0.003, 0.001, 0.0003):
-        mst = _time_steps(lambda: sur.wdot(Te, Pe, Ye, tol=tl, out=out), 2, 1, stream, dist)
-        wt, nf = sur.wdot(Te, Pe, Ye, tol=tl, out=out)
-        et = q(((wt - exact).abs() / den).amax(dim=0))
-        sweep.append({"tol": tl, "fallback_fraction": nf / ne,
-                      "states_per_s": ne * world / (mst * 1e-3), "error": et})
+    for bd in (0.05, 0.1, 0.2, 0.5):
+        st = sur.threshold(g_cal, e_cal, margin * bd)
+        mst = _time_steps(lambda: sur.wdot(Te, Pe, Ye, stol=st, out=out), 2, 3, stream, dist)
+        wt, nf = sur.wdot(Te, Pe, Ye, stol=st, out=out)
+        et = q(sur.served_error(wt, exact))
+        sweep.append({"bound": bd, "stol": st, "fallback_fraction": nf / ne,
+                      "states_per_s": ne * world / (mst * 1e-3), "error": et,
+                      "bound_held": bool(et["max"] <= bd)})
     peak = None
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -639,14 +659,23 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
     inf_tflops = 2.0 * macs * ne / (ms_inf * 1e-3) / 1e12
     fused = net.fused_ok()
     res = {
-        "network": "MLP %s, SiLU, bf16 weights / fp32 accumulation, tcgen05 GEMMs"
-                   % "->".join(str(d) for d in net.dims),
+        "network": "2 x MLP %s (served: their mean), SiLU, bf16 weights / fp32 accumulation, "
+                   "tcgen05 GEMMs; error network %s"
+                   % ("->".join(str(d) for d in net.dims),
+                      "->".join(str(d) for d in sur.err_net.dims)),
         "train_states": n_tr, "epochs": args.sur_epochs, "batch": B,
         "train_loss_per_epoch": losses, "fit_seconds": fit_s,
+        "gate_fit_states": args.sur_gate_states, "gate_fit_seconds": gate_fit_s,
+        "gate_loss_per_epoch": gate_losses,
         "train_step_ms": ms_step,
         "train_states_per_s": B * world / (ms_step * 1e-3),
         "train_tflops": train_flops_state * B / (ms_step * 1e-3) / 1e12,
-        "eval_states": ne, "tol": tol,
+        "eval_states": ne,
+        "bound": bound, "stol": stol,
+        "calibration": {"states": int(g_cal.numel()), "margin": margin,
+                        "fallback_fraction": 1.0 - float((g_cal <= stol).double().mean()),
+                        "rule": "largest score up to which every calibration state has "
+                                "error <= margin x bound"},
         "value": ne * world / (ms_sur * 1e-3), "unit": "states/s",
         "ms_per_step": ms_sur,
         "network_only_states_per_s": ne * world / (ms_net * 1e-3),
@@ -654,22 +683,24 @@ def _bench_surrogate(args, rs, stream, dist, world, rank):
         "mixed_states_per_s": ne * world / (ms_mixed * 1e-3),
         "speedup_vs_plain": ms_plain / ms_sur,
         "fallback_fraction": nfb / ne,
+        "bound_held": bool(err_gated["max"] <= bound),
         "error_definition": "per state max_k |w_k - w_k,fp64| / (|w_k,fp64| + s_k), "
                             "s_k = std of wdot_k over the training states",
         "error_gated": err_gated, "error_network_all_states": err_raw,
         "error_network_served_states": err_served,
-        "gate_sweep": sweep,
+        "bound_sweep": sweep,
         "roofline": {"bound": "tensor",
                      "kernel": ("network inference, all layers in one kernel (crs_mlp_infer)"
                                 if fused else "network forward, one tcgen05 GEMM per layer"),
                      "achieved": inf_tflops, "peak": peak, "unit": "TFLOP/s",
                      "frac": inf_tflops / peak, "flops_per_state": 2 * macs,
+                     "gated_path_flops_per_state": 2 * (2 * macs + emacs),
                      "peak_note": "bf16 burst, of measured",
                      "layer_by_layer": {"achieved": fwd_tflops, "frac": fwd_tflops / peak,
                                         "ms": ms_fwd},
                      "fused_ms": ms_inf},
     }
-    del Te, Pe, Ye, out, exact, w, raw, den, e_raw, served, wt
+    del Te, Pe, Ye, out, exact, w, raw, e_raw, served, wt, g_cal, e_cal
     return res
 
 
@@ -695,11 +726,11 @@ def _bench_large(args, stream, dist, world, peaks, rank):
                         "(254 three-body, 127 Troe, 156 irreversible)",
            "n_states": n, "modes": {}}
     sub = 4096
-    steps = max(3, args.steps // 2)
+    steps = max(5, args.steps // 2)
     got = {}
     precision = {"fp64": "fp64", "mixed": "mixed", "gemm": "rates"}
     for mode in ("fp64", "mixed", "gemm"):
-        ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), steps, 2, stream, dist)
+        ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), steps, 3, stream, dist)
         got[mode] = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], mode).cpu().numpy()
         sps = n / (ms * 1e-3)
         res["modes"][mode] = {"value": n * world / (ms * 1e-3), "unit": "states/s",

@@ -86,6 +86,9 @@ def _sig(lib):
                                    _i64, _vp, _i64, _i32, _vp, _vp, _vp],
         "crs_surrogate_output": [_i64, _vp, _i64, _i32, _vp, _vp, _vp, _i32, ctypes.c_float,
                                  _vp, _vp, _i64, _vp, _vp],
+        "crs_surrogate_output2": [_i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _i32,
+                                  ctypes.c_float, _vp, _i64, ctypes.c_float, _vp,
+                                  _vp, _i64, _vp, _vp, _vp],
         "crs_select": [_i64, _vp, _vp, _vp, _vp],
         "crs_gather_states": [_i64, _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp],
         "crs_scatter_wdot": [_i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp],

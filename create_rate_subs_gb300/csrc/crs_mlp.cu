@@ -331,6 +331,53 @@ __global__ void k_output(int64_t n, const float *Yh, int64_t ldy, int nsp, const
   }
 }
 
+// Two-member output with an error gate.  The served y_k is the mean of the
+// members' outputs; in y = sign(u) log1p|u| space a change dy moves w by
+// |dy| (|w| + s) to first order, so an error in y is the reported error
+// e = max_k |w_k - w_k,exact| / (|w_k,exact| + s_k).  The gate score of a
+// state is
+//   g = log10(D + 1e-4) + E,   D = max_k |y_k,a - y_k,b|,
+// the members' disagreement plus E = est[i * lde], the output of a network
+// trained to predict log10(e + 1e-4) (omitted when est is NULL).  A state
+// goes back to the exact kernel as in k_output, or when g > stol (NaN
+// included).  gate[i] (optional) receives g, for calibrating stol.
+__global__ void k_output2(int64_t n, const float *Ya, const float *Yb, int64_t ldy, int nsp,
+                          const float *sm, const int *se, const float *cons, int nelem,
+                          float tol, const float *est, int64_t lde, float stol,
+                          const unsigned char *out_of_box, double *wdot, int64_t ld,
+                          unsigned char *fallback, float *gate) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float sum[MAX_ELEM], mag[MAX_ELEM];
+#pragma unroll
+    for (int e = 0; e < MAX_ELEM; ++e) sum[e] = mag[e] = 0.0f;
+    float d = 0.0f;
+    for (int k = 0; k < nsp; ++k) {
+      const float ya = Ya[i * ldy + k], yb = Yb[i * ldy + k];
+      d = fmaxf(d, fabsf(ya - yb));
+      const float y = 0.5f * (ya + yb);
+      const float u = copysignf(expm1f(fabsf(y)), y);
+      wdot[(int64_t)k * ld + i] = scale_to_double(u * sm[k], se[k]);
+#pragma unroll
+      for (int e = 0; e < MAX_ELEM; ++e) {
+        if (e < nelem) {
+          const float c = cons[e * nsp + k];
+          sum[e] = fmaf(c, u, sum[e]);
+          mag[e] = fmaf(c, fabsf(u) + 1.0f, mag[e]);
+        }
+      }
+    }
+    float worst = 0.0f;
+#pragma unroll
+    for (int e = 0; e < MAX_ELEM; ++e)
+      if (e < nelem && mag[e] > 0.0f) worst = fmaxf(worst, fabsf(sum[e]) / mag[e]);
+    const float g = log10f(d + 1.0e-4f) + (est ? est[i * lde] : 0.0f);
+    const bool fb = !(worst <= tol) || !(g <= stol) || (out_of_box && out_of_box[i]);
+    fallback[i] = fb;
+    if (gate) gate[i] = g;
+  }
+}
+
 // Indices of flagged states (order unspecified; one warp-aggregated atomic
 // per warp).  count must be zero on entry.
 __global__ void k_compact(int64_t n, const unsigned char *flag, int64_t *idx,
@@ -519,6 +566,22 @@ int crs_surrogate_output(int64_t n, const float *Yh, int64_t ldy, int nsp, const
   if (n == 0) return CRS_OK;
   mlp::k_output<<<mlp::grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       n, Yh, ldy, nsp, scale_m, scale_e, cons, nelem, tol, out_of_box, wdot, ld, fallback);
+  return done(cudaGetLastError(), __func__);
+}
+
+int crs_surrogate_output2(int64_t n, const float *Ya, const float *Yb, int64_t ldy, int nsp,
+                          const float *scale_m, const int *scale_e, const float *cons, int nelem,
+                          float tol, const float *est, int64_t lde, float stol,
+                          const unsigned char *out_of_box, double *wdot, int64_t ld,
+                          unsigned char *fallback, float *gate, void *stream) {
+  if (n < 0 || !Ya || !Yb || !scale_m || !scale_e || !wdot || !fallback ||
+      (nelem && !cons) || nelem < 0 || nelem > mlp::MAX_ELEM || ld < n || ldy < nsp ||
+      (est && lde < 1))
+    return bad(__func__);
+  if (n == 0) return CRS_OK;
+  mlp::k_output2<<<mlp::grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      n, Ya, Yb, ldy, nsp, scale_m, scale_e, cons, nelem, tol, est, lde, stol, out_of_box,
+      wdot, ld, fallback, gate);
   return done(cudaGetLastError(), __func__);
 }
 

@@ -1,18 +1,25 @@
 """Learned surrogate for wdot with exact fallback.
 
-A multilayer perceptron maps a state's features -- T, ln P and
+Two multilayer perceptrons ("members", different initial weights and batch
+order, same training states) map a state's features -- T, ln P and
 ln(Y_k + 1e-12) for every species, standardised -- to the species
 production rates, each normalised by its standard deviation over the
 training states and passed through sign(x) log(1 + |x|):
 
     y_k = sign(w_k / s_k) log1p(|w_k| / s_k),   s_k = std(w_k)
 
-The default network is 55 -> 256 -> 256 -> 256 -> 53 (SiLU) for the
-53-species mechanism.  Weights are bf16 on the tensor cores with fp32
-accumulation and fp32 master copies; training (forward, backward, Adam)
-and inference run entirely in libcrs's own kernels (crs_mlp_*,
-crs_adam_step, crs_surrogate_*).  Training states are drawn like the
-benchmark states and labelled by the exact FP64 kernel.
+The served y is the members' mean.  The default network is
+55 -> 256 -> 256 -> 256 -> 53 (SiLU) for the 53-species mechanism.  Weights
+are bf16 on the tensor cores with fp32 accumulation and fp32 master
+copies; training (forward, backward, Adam) and inference run entirely in
+libcrs's own kernels (crs_mlp_*, crs_adam_step, crs_surrogate_*).
+Training states are drawn like the benchmark states and labelled by the
+exact FP64 kernel.
+
+Error measure reported for the surrogate: e = max_k |w_k - w_k,exact| /
+(|w_k,exact| + s_k), i.e. relative error where a rate is large and error in
+units of the species' typical rate where it is small.  In y space a change
+dy moves w by |dy| (|w| + s) to first order, so e is about max_k |dy_k|.
 
 Every evaluation is gated.  A state goes back to the exact kernel
 (CRS_MODE_FP64 on the gathered states, results scattered into place) when
@@ -20,12 +27,17 @@ Every evaluation is gated.  A state goes back to the exact kernel
 * one of its features lies outside the box spanned by the training states
   (widened by 2 % of each feature's range), or
 * its element residual max_e |sum_k a_ek w_k| / sum_k a_ek (|w_k| + s_k)
-  exceeds ``tol``: exact production rates conserve every element, so a
-  residual is a measured symptom of surrogate error.
+  exceeds ``tol`` (exact production rates conserve every element), or
+* its error score g = log10(D + 1e-4) + E exceeds ``stol``: D is the
+  members' disagreement max_k |y_k,a - y_k,b|, E the output of an error
+  network (55 -> 256 -> 256 -> 1) trained on held-out states, labelled by
+  the exact kernel, to predict log10(e + 1e-4) of the served result.
 
-Error measure reported for the surrogate: e = max_k |w_k - w_k,exact| /
-(|w_k,exact| + s_k), i.e. relative error where a rate is large and error in
-units of the species' typical rate where it is small.
+``calibrate(bound)`` sets ``stol`` from a further held-out set labelled by
+the exact kernel: the largest score up to which every calibration state
+has e <= margin * bound (margin 0.5 by default).  The plain kernel is thus both the fallback and the judge
+of the surrogate's error; the bound holds on the calibration states and is
+measured again on fresh states by the tests and bench.py.
 
 The reference has no surrogate; this module is the learned part that sits
 beside its four functions.
@@ -277,21 +289,33 @@ def surrogate_error(w, w_exact, scale):
 
 
 class Surrogate(object):
-    """wdot(T, P, Y) from the trained network, with exact fallback.
+    """wdot(T, P, Y) from the trained networks, with gated exact fallback.
 
-    ``rs`` is a RateSubs (the exact kernel: labels and fallback)."""
+    ``rs`` is a RateSubs (the exact kernel: labels, fallback and judge).
+    ``members``: 2 (served y = mean of two networks, their disagreement in
+    the gate) or 1."""
 
-    def __init__(self, rs, hidden=(256, 256, 256), seed=0, batch=16384):
+    def __init__(self, rs, hidden=(256, 256, 256), seed=0, batch=16384, members=2,
+                 err_hidden=(256, 256)):
         torch = _torch()
         if rs.mech is None:
             raise ValueError("the surrogate needs the Mechanism (element counts)")
+        if members not in (1, 2):
+            raise ValueError("members must be 1 or 2")
         self.rs = rs
         self.lib = rs.lib
         self.device = rs.device
         N = rs.n_species
         self.N = N
         self.n_in = 2 + N
-        self.net = MLP([self.n_in] + list(hidden) + [N], seed=seed, device=self.device)
+        self.nets = [MLP([self.n_in] + list(hidden) + [N], seed=seed + 7919 * j,
+                         device=self.device) for j in range(members)]
+        self.net = self.nets[0]
+        self.err_net = MLP([self.n_in] + list(err_hidden) + [1], seed=seed + 104729,
+                           device=self.device)
+        self.err_trained = False
+        self.stol = float("inf")   # gate threshold on the error score
+        self.bound = None          # the calibrated error bound, if any
         self.batch = int(batch)
         if self.batch % 128:
             raise ValueError("batch must be a multiple of 128")
@@ -354,10 +378,43 @@ class Surrogate(object):
         x = W / self.scale[:, None]
         return (torch.sign(x) * torch.log1p(torch.abs(x))).t().contiguous().float()
 
+    def _batches(self, T, P, Y, n):
+        """Features of n states (a multiple of the batch) as X (n, pad) and
+        the per-batch transposes XT (nb, pad, B) that training reads."""
+        torch = _torch()
+        B = self.batch
+        nb = n // B
+        X = torch.zeros((n, self.net.pad[0]), dtype=torch.bfloat16, device=self.device)
+        XT = torch.zeros((nb, self.net.pad[0], B), dtype=torch.bfloat16, device=self.device)
+        for j in range(nb):
+            o = j * B
+            self.features(T[o:], P[o:], Y[:, o:], Y.stride(0), B, X[o:], XT[j], B, box=False)
+        return X, XT
+
+    def _train(self, net, X, XT, Tg, epochs, lr, lr_final, seed):
+        """Adam with a cosine learning-rate schedule over shuffled batches;
+        returns the mean loss per epoch."""
+        torch = _torch()
+        B = self.batch
+        nb = X.shape[0] // B
+        losses = torch.zeros(epochs * nb, dtype=torch.float32, device=self.device)
+        rng = np.random.default_rng(seed)
+        total = epochs * nb
+        for e in range(epochs):
+            order = rng.permutation(nb)
+            for i, j in enumerate(order):
+                st = e * nb + i
+                lr_s = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * st / total))
+                o = int(j) * B
+                net.train_step(X[o:o + B], XT[int(j)], Tg[o:o + B], lr_s,
+                               loss_slot=losses[st:st + 1])
+        return losses.view(epochs, nb).mean(dim=1).cpu().numpy().tolist()
+
     # -- training --------------------------------------------------------
     def fit(self, n_train=1 << 20, epochs=4, lr=1e-3, lr_final=1e-5, seed=1,
             states=None):
-        """Label n_train states with the exact kernel and train.  Returns the
+        """Label n_train states with the exact kernel and train every member
+        on them (member j shuffles with seed + j).  Returns the members'
         mean training loss per epoch."""
         torch = _torch()
         B = self.batch
@@ -381,52 +438,113 @@ class Surrogate(object):
         lo, hi = raw.min(dim=0).values, raw.max(dim=0).values
         self.lo.copy_(lo - 0.02 * (hi - lo))
         self.hi.copy_(hi + 0.02 * (hi - lo))
-        del raw
-        nb = n // B
-        XT = torch.zeros((nb, self.net.pad[0], B), dtype=torch.bfloat16, device=self.device)
-        for j in range(nb):
-            o = j * B
-            self.features(T[o:], P[o:], Y[:, o:], n, B, X[o:], XT[j], B, box=False)
+        del raw, X
+        X, XT = self._batches(T, P, Y, n)
         Tg = self.targets(W)
         del W
-        losses = torch.zeros(epochs * nb, **f32)
-        rng = np.random.default_rng(seed)
-        total = epochs * nb
-        for e in range(epochs):
-            order = rng.permutation(nb)
-            for i, j in enumerate(order):
-                s = e * nb + i
-                lr_s = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * s / total))
-                o = int(j) * B
-                self.net.train_step(X[o:o + B], XT[int(j)], Tg[o:o + B], lr_s,
-                                    loss_slot=losses[s:s + 1])
-        per_epoch = losses.view(epochs, nb).mean(dim=1).cpu().numpy().tolist()
+        per = [self._train(net, X, XT, Tg, epochs, lr, lr_final, seed + j)
+               for j, net in enumerate(self.nets)]
+        per_epoch = np.mean(np.array(per), axis=0).tolist()
         self.history.extend(per_epoch)
+        # the error network and the gate threshold belong to the old weights
+        self.err_trained = False
+        self.stol, self.bound = float("inf"), None
         return per_epoch
 
-    def loss(self, T, P, Y):
-        """Mean squared error of the network on states (exact labels)."""
+    def served_error(self, w, W):
+        """Per-state e = max_k |w_k - W_k| / (|W_k| + s_k) (device, (n,))."""
+        return ((w - W).abs() / (W.abs() + self.scale[:, None])).amax(dim=0)
+
+    def fit_gate(self, n=1 << 22, epochs=12, lr=2e-3, lr_final=2e-5, seed=2, states=None):
+        """Train the error network on n held-out states (seed: their draw,
+        unless ``states`` is given) labelled by the exact kernel: target
+        log10(e + 1e-4), e the error of the served (members' mean) result.
+        Returns the loss per epoch."""
         torch = _torch()
+        B = self.batch
+        n = _r(n, B)
+        T, P, Y = states if states is not None else self.sample_states(n, seed)
         n = T.shape[0]
+        if n % B:
+            raise ValueError("number of states must be a multiple of the batch")
+        Yr = Y[: self.N - 1].contiguous()
+        W = self.rs.wdot(T, P, Yr, mode="fp64")
+        w, _, _ = self._serve(T, P, Yr, stol=float("inf"), use_err=False)
+        tgt = torch.log10(self.served_error(w, W) + 1e-4).float()[:, None].contiguous()
+        del W, w
+        X, XT = self._batches(T, P, Y, n)
+        losses = self._train(self.err_net, X, XT, tgt, epochs, lr, lr_final, seed)
+        self.err_trained = True
+        return losses
+
+    def gate_scores(self, T, P, Y):
+        """(served wdot (N, n), gate score g (n,), error e (n,)) of the
+        network path on states labelled here by the exact kernel."""
+        Yr = Y[: self.N - 1].contiguous() if Y.shape[0] == self.N else Y
+        W = self.rs.wdot(T, P, Yr, mode="fp64")
+        w, _, g = self._serve(T, P, Yr, stol=float("inf"))
+        return w, g, self.served_error(w, W)
+
+    @staticmethod
+    def threshold(g, e, bound):
+        """Largest score such that every state scoring at or below it has
+        e <= bound (-inf when even the best-scored state exceeds it)."""
+        torch = _torch()
+        order = torch.argsort(g)
+        bad = torch.nonzero(e[order] > bound)
+        first = int(bad[0]) if bad.numel() else int(g.numel())
+        if first == 0:
+            return float("-inf")
+        # states tied with the first bad score must not be served
+        tau = float(g[order[first - 1]])
+        if first < g.numel() and float(g[order[first]]) == tau:
+            below = g[order[:first]] < tau
+            tau = float(g[order[:first]][below].max()) if bool(below.any()) else float("-inf")
+        return tau
+
+    def calibrate(self, bound, n=1 << 22, seed=3, margin=0.5, states=None):
+        """Set the gate threshold ``stol`` so that every one of n held-out
+        states labelled by the exact kernel that the network would serve has
+        e <= margin * bound.  The margin covers the tail of fresh states: a
+        threshold calibrated at the bound itself on 2^22 states let errors
+        up to 1.65x the bound through on 2^24 fresh ones.  Returns the
+        calibration summary."""
+        torch = _torch()
+        T, P, Y = states if states is not None else self.sample_states(n, seed)
+        _, g, e = self.gate_scores(T, P, Y)
+        tau = self.threshold(g, e, margin * bound)
+        self.stol, self.bound = tau, float(bound)
+        served = g <= tau
+        return {"bound": float(bound), "margin": float(margin), "stol": tau,
+                "states": int(g.numel()),
+                "fallback_fraction": 1.0 - float(served.double().mean()),
+                "served_max": float(e[served].max()) if bool(served.any()) else 0.0}
+
+    def loss(self, T, P, Y):
+        """Mean squared error of the served network output on states
+        (exact labels)."""
         W = self.rs.wdot(T, P, Y, mode="fp64")
         Yh = self.predict(T, P, Y)
         return float(((Yh - self.targets(W)) ** 2).mean())
 
     def predict(self, T, P, Y):
-        """Raw network outputs (n, N) fp32."""
+        """Served network outputs (n, N) fp32: the members' mean."""
         torch = _torch()
         n = T.shape[0]
         M = _r(max(n, 1), 128)
         X = torch.zeros((M, self.net.pad[0]), dtype=torch.bfloat16, device=self.device)
         self.features(T, P, Y, Y.stride(0), n, X, box=False)
-        Yh = torch.empty((n, self.net.pad[-1]), dtype=torch.float32, device=self.device)
-        self.net.infer(X, n, Yh)
-        return Yh[:, : self.N]
+        acc = None
+        for net in self.nets:
+            Yh = torch.empty((n, net.pad[-1]), dtype=torch.float32, device=self.device)
+            net.infer(X, n, Yh)
+            acc = Yh[:, : self.N] if acc is None else acc + Yh[:, : self.N]
+        return acc / len(self.nets)
 
     # -- evaluation ------------------------------------------------------
-    def wdot(self, T, P, Y, tol=0.05, out=None, with_fallback=True):
-        """wdot (N, n) for every state: the network where the gate passes,
-        the exact FP64 kernel elsewhere.  Returns (wdot, n_fallback)."""
+    def _serve(self, T, P, Y, tol=float("inf"), stol=None, out=None, use_err=True):
+        """The network path: (wdot (N, n), fallback flags (n,) uint8, gate
+        score (n,)).  Y holds the N - 1 independent mass fractions."""
         torch = _torch()
         n, ld = self.rs._check_states(T, P, Y)
         s = _stream(self.device)
@@ -435,21 +553,44 @@ class Surrogate(object):
             out = torch.empty((N, n), dtype=torch.float64, device=self.device)
         elif out.shape != (N, n) or not out.is_contiguous():
             raise ValueError("out must be a contiguous (species, n) float64 tensor")
+        stol = self.stol if stol is None else stol
+        f32 = dict(dtype=torch.float32, device=self.device)
+        flag = torch.empty(n, dtype=torch.uint8, device=self.device)
+        gate = torch.empty(n, **f32)
+        if n == 0:
+            return out, flag, gate
+        M = _r(n, 128)
+        X = torch.empty((M, self.net.pad[0]), dtype=torch.bfloat16, device=self.device)
+        box = torch.empty(n, dtype=torch.uint8, device=self.device)
+        self.features(T, P, Y, ld, n, X, out_of_box=box)
+        Yh = [torch.empty((n, net.pad[-1]), **f32) for net in self.nets]
+        for net, y in zip(self.nets, Yh):
+            net.infer(X, n, y, s)
+        est = None
+        if use_err and self.err_trained:
+            est = torch.empty((n, 4), **f32)
+            self.err_net.infer(X, n, est, s)
+        _lib.check(self.lib.crs_surrogate_output2(
+            n, _p(Yh[0]), _p(Yh[-1]), Yh[0].stride(0), N, _p(self._scale_m), _p(self._scale_e),
+            _p(self._cons), self.n_elem, tol, _p(est), est.stride(0) if est is not None else 0,
+            stol, _p(box), _p(out), n, _p(flag), _p(gate), s))
+        return out, flag, gate
+
+    def wdot(self, T, P, Y, tol=0.05, stol=None, out=None, with_fallback=True):
+        """wdot (N, n) for every state: the networks where the gate passes,
+        the exact FP64 kernel elsewhere.  ``stol``: gate threshold on the
+        error score (default: the calibrated one; infinite before
+        ``calibrate``).  Returns (wdot, n_fallback)."""
+        torch = _torch()
+        out, flag, _ = self._serve(T, P, Y, tol=tol, stol=stol, out=out)
+        n = out.shape[1]
         if n == 0:
             return out, 0
-        M = _r(n, 128)
-        u8 = dict(dtype=torch.uint8, device=self.device)
-        X = torch.empty((M, self.net.pad[0]), dtype=torch.bfloat16, device=self.device)
-        box = torch.empty(n, **u8)
-        flag = torch.empty(n, **u8)
-        self.features(T, P, Y, ld, n, X, out_of_box=box)
-        Yh = torch.empty((n, self.net.pad[-1]), dtype=torch.float32, device=self.device)
-        self.net.infer(X, n, Yh, s)
-        _lib.check(self.lib.crs_surrogate_output(
-            n, _p(Yh), Yh.stride(0), N, _p(self._scale_m), _p(self._scale_e), _p(self._cons), self.n_elem,
-            tol, _p(box), _p(out), n, _p(flag), s))
         if not with_fallback:
             return out, int(flag.sum())
+        s = _stream(self.device)
+        N = self.N
+        ld = Y.stride(0)
         idx = torch.empty(n, dtype=torch.int64, device=self.device)
         cnt = torch.zeros(1, dtype=torch.int64, device=self.device)
         _lib.check(self.lib.crs_select(n, _p(flag), _p(idx), _p(cnt), s))
@@ -465,17 +606,30 @@ class Surrogate(object):
         return out, m
 
     def save(self, path):
-        d = self.net.state_dict()
+        d = {}
+        for j, net in enumerate(self.nets):
+            for k, v in net.state_dict().items():
+                d["m%d_%s" % (j, k)] = v
+        for k, v in self.err_net.state_dict().items():
+            d["err_%s" % k] = v
         for k in ("mu", "sd", "lo", "hi", "scale"):
             d[k] = getattr(self, k).cpu().numpy()
         d["history"] = np.array(self.history)
+        d["gate"] = np.array([self.stol, np.nan if self.bound is None else self.bound,
+                              float(self.err_trained)])
         np.savez(path, **d)
 
     def load(self, path):
         torch = _torch()
         d = dict(np.load(path))
-        self.net.load_state_dict(d)
+        for j, net in enumerate(self.nets):
+            net.load_state_dict({k[len("m%d_" % j):]: v for k, v in d.items()
+                                 if k.startswith("m%d_" % j)})
+        self.err_net.load_state_dict({k[4:]: v for k, v in d.items() if k.startswith("err_")})
         for k in ("mu", "sd", "lo", "hi"):
             getattr(self, k).copy_(torch.from_numpy(d[k]))
         self.set_scale(d["scale"])
         self.history = list(d.get("history", []))
+        stol, bound, trained = (float(x) for x in d["gate"])
+        self.stol, self.bound = stol, (None if math.isnan(bound) else bound)
+        self.err_trained = bool(trained)

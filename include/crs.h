@@ -304,6 +304,21 @@ int crs_surrogate_output(int64_t n, const float *Yh, int64_t ldy, int nsp,
                          const float *cons, int nelem, float tol,
                          const unsigned char *out_of_box, double *wdot,
                          int64_t ld, unsigned char *fallback, void *stream);
+/* Two-network form of crs_surrogate_output with an error gate (no
+ * counterpart in the reference).  Ya and Yb are two networks' outputs
+ * (same layout); the served y is their mean.  Gate score of state i:
+ * g = log10(D + 1e-4) + est[i * lde], D = max_k |Ya[i][k] - Yb[i][k]| (the
+ * networks' disagreement) and est the output of an error network trained
+ * to predict log10 of the served error + 1e-4 (may be NULL: term omitted).
+ * fallback[i] = 1 as in crs_surrogate_output, or when g > stol (NaN
+ * included).  gate (may be NULL) receives g. */
+int crs_surrogate_output2(int64_t n, const float *Ya, const float *Yb,
+                          int64_t ldy, int nsp, const float *scale_m,
+                          const int *scale_e, const float *cons, int nelem,
+                          float tol, const float *est, int64_t lde, float stol,
+                          const unsigned char *out_of_box, double *wdot,
+                          int64_t ld, unsigned char *fallback, float *gate,
+                          void *stream);
 /* idx[0..count) = the i < n with flag[i] != 0, in no particular order
  * (count: device int64, set by the call). */
 int crs_select(int64_t n, const unsigned char *flag, int64_t *idx,
