@@ -87,8 +87,10 @@ def _sig(lib):
         "crs_surrogate_output": [_i64, _vp, _i64, _i32, _vp, _vp, _vp, _i32, ctypes.c_float,
                                  _vp, _vp, _i64, _vp, _vp],
         "crs_surrogate_output2": [_i64, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _i32,
-                                  ctypes.c_float, _vp, _i64, ctypes.c_float, _vp,
-                                  _vp, _i64, _vp, _vp, _vp],
+                                  ctypes.c_float, ctypes.c_float, _vp, _i64, ctypes.c_float,
+                                  _vp, _vp, _i64, _vp, _vp, _vp],
+        "crs_surrogate_disagreement": [_i64, _vp, _vp, _i64, _i32, ctypes.c_float,
+                                       ctypes.c_float, _vp, _i64, _i32, _vp],
         "crs_select": [_i64, _vp, _vp, _vp, _vp],
         "crs_gather_states": [_i64, _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp],
         "crs_scatter_wdot": [_i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp],

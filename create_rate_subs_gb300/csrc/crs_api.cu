@@ -341,7 +341,9 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   for (int e = 0; e < t.nu_ptr[L.R]; ++e) {
     uint64_t u;
     memcpy(&u, &t.nu_val[e], 8);
-    L.nu_hi_exact &= (u & 0xffffffffull) == 0;
+    // the double is its top 16 bits followed by zeros (small integers,
+    // halves, ...): the compact nu list holds exactly those 16 bits
+    L.nu_hi_exact &= (u & 0x0000ffffffffffffull) == 0;
   }
   using M = int crs::ImgLayout::*;
   std::vector<std::pair<M, std::vector<unsigned char>>> secs;
@@ -401,7 +403,7 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   raw(&IL::pm_kinf, "pm_kinf"); raw(&IL::pm_troe_t2, "pm_troe_t2");
   raw(&IL::pm_sri_de, "pm_sri_de");
   der(&IL::troe_x); der(&IL::sri_x); der(&IL::troe_ff); der(&IL::sri_ff);
-  der(&IL::eff_f);
+  der(&IL::eff_f); der(&IL::logtab);
   raw(&IL::rate_par, "rate_par"); raw(&IL::kc_pref, "kc_pref");
   raw(&IL::pm_troe, "pm_troe"); raw(&IL::pm_sri, "pm_sri");
   raw(&IL::kc_dnu, "kc_dnu"); raw(&IL::sp_lo, "sp_lo"); raw(&IL::sp_hi, "sp_hi");
@@ -1013,21 +1015,61 @@ int crs_dydt(const crs_mech *m, int64_t n, const double *p_or_rho, const double 
   return result;
 }
 
+}  // extern "C"
+
+namespace {
+// The device address of a host array that the current device can read and
+// write in place (page-locked memory mapped into its address space), else
+// null.
+void *mapped_view(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+}  // namespace
+
+extern "C" {
+
 int crs_wdot_host(const crs_mech *m, int64_t n, const double *T, const double *P,
                   const double *Y, int64_t ld, double *wdot, int mode) {
   int rc = check_batch(m, n, ld);
   if (rc) return rc;
   if (n == 0) return CRS_OK;
   if (!T || !P || !Y || !wdot) return fail(CRS_ERR_ARG, "NULL array");
+  const bool staged_only = (mode & CRS_HOST_STAGED) != 0;
+  mode &= ~CRS_HOST_STAGED;
   crs_mech *mm = const_cast<crs_mech *>(m);
   std::lock_guard<std::mutex> lock(mm->host_mu);
   const int64_t N = m->L.N;
+  cudaError_t e = cudaSuccess;
+  if (!mm->hs[0]) e = cudaStreamCreateWithFlags(&mm->hs[0], cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "crs_wdot_host streams");
+  if (!staged_only) {
+    // arrays the device addresses in place: one launch reads the states
+    // from host memory and writes wdot back over the host link (NVLink-C2C
+    // on Grace), without staging copies or per-chunk launches
+    void *vT = mapped_view(T), *vP = mapped_view(P), *vY = mapped_view(Y),
+         *vW = mapped_view(wdot);
+    if (vT && vP && vY && vW) {
+      crs::Batch b = make_batch(m, n, ld);
+      b.T = static_cast<const double *>(vT);
+      b.P = static_cast<const double *>(vP);
+      b.Y = static_cast<const double *>(vY);
+      b.wdot = static_cast<double *>(vW);
+      int result = launch_mode(m, b, mode, mm->hs[0]);
+      const cudaError_t es = cudaStreamSynchronize(mm->hs[0]);
+      if (es != cudaSuccess && result == CRS_OK) result = cuda_fail(es, "crs_wdot_host");
+      return result;
+    }
+  }
   const int64_t per = 2 + (N - 1) + N;  // doubles per state: T, P, Y, wdot
   // chunks of up to 2^17 states, at most 256 MB per buffer
   int64_t chunk = ((int64_t)256 << 20) / (per * 8);
   if (chunk > ((int64_t)1 << 17)) chunk = (int64_t)1 << 17;
   if (chunk < 128) chunk = 128;
-  cudaError_t e = cudaSuccess;
   if (mm->host_chunk < chunk) {
     if (mm->d_host) cudaFree(mm->d_host);
     mm->d_host = nullptr;

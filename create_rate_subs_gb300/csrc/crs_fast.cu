@@ -91,6 +91,13 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   }
   std::vector<double> et(256);
   for (int j = 0; j < 256; ++j) et[j] = (double)exp2l((long double)j / 256.0L);
+  // (1/F, log F) for F = 1 + j/128 of the table logarithm (texp::log_t)
+  std::vector<double> lt(2 * texp::LOG_TAB_ENTRIES);
+  for (int j = 0; j < texp::LOG_TAB_ENTRIES; ++j) {
+    const long double F = 1.0L + (long double)j / 128.0L;
+    lt[2 * j] = (double)(1.0L / F);
+    lt[2 * j + 1] = (double)logl(F);
+  }
   put(extra, &ImgLayout::rate_x, rx);
   put(extra, &ImgLayout::kc_lpref, lp);
   // Kc polynomials with the prefactor folded in (single T_common group)
@@ -137,6 +144,7 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   put(extra, &ImgLayout::sri_x, sx);
   put(extra, &ImgLayout::sp_gibbs, g);
   put(extra, &ImgLayout::exptab, et);
+  put(extra, &ImgLayout::logtab, lt);
   // mixed-precision tables
   auto split = [](double v, float *h, float *l) {
     *h = (float)v;
@@ -234,12 +242,12 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   {
     const int nnz = t.nu_ptr[L.R];
     std::vector<int16_t> sp16(nnz > 0 ? nnz : 1, 0);
-    std::vector<int32_t> hi(nnz > 0 ? nnz : 1, 0);
+    std::vector<uint16_t> hi(nnz > 0 ? nnz : 1, 0);
     for (int e = 0; e < nnz; ++e) {
       uint64_t u;
       memcpy(&u, &t.nu_val[e], 8);
       sp16[e] = (int16_t)t.nu_sp[e];
-      hi[e] = (int32_t)(u >> 32);
+      hi[e] = (uint16_t)(u >> 48);  // the top 16 bits of the double
     }
     put(extra, &ImgLayout::nu_sp16, sp16);
     put(extra, &ImgLayout::nu_hi, hi);
@@ -316,6 +324,7 @@ namespace fast {
 using texp::exp_core;
 using texp::exp_fix;
 using texp::exp_t;
+using texp::log_t;
 constexpr double INV_RU = 0.0001202723625380408;
 constexpr double LN10 = 2.302585092994046;
 constexpr double INV_LN10 = 0.4342944819032518;
@@ -350,7 +359,8 @@ struct IsKcCol<KcCol<CS>> { static constexpr bool value = true; };
 
 struct State {
   double T, invT, logT, P;
-  const double *tab;
+  const double *tab;   // 2^(j/256), exp_t
+  const double *ltab;  // (1/F, log F), log_t
 };
 
 // Rate constant of row `row`; *x receives its exponent for the EXP kind.
@@ -420,21 +430,24 @@ __device__ double pres_mod(const Tab &t, int p, const State &s, double mix,
   const double inv1p = 1.0 / (1.0 + Pr);
   const int form = t.pm_form[p];
   if (form == FORM_LINDEMANN) return low ? Pr * inv1p : inv1p;
-  const double lP = log(fmax(Pr, 1.0e-300)) * INV_LN10;
+  const double lP = log_t(fmax(Pr, 1.0e-300), s.ltab) * INV_LN10;
   double F;
   if (form == FORM_TROE) {
     const double *c = t.troe_x + 5 * p;  // P0, -1/T3, P2, -1/T1, -T2
     double f = c[0] * exp_t(s.T * c[1], s.tab) + c[2] * exp_t(s.T * c[3], s.tab);
     if (t.pm_troe_t2[p]) f += exp_t(c[4] * s.invT, s.tab);
-    const double lF = log(fmax(f, 1.0e-300)) * INV_LN10;
+    const double lF = log_t(fmax(f, 1.0e-300), s.ltab) * INV_LN10;
     const double A = lP - 0.67 * lF - 0.4;
     const double B = 0.806 - 1.1762 * lF - 0.14 * lP;
-    F = exp_t(LN10 * lF / (1.0 + A * A / (B * B)), s.tab);
+    // log10 F = log10 Fcent / (1 + A^2/B^2) = log10 Fcent B^2 / (B^2 + A^2):
+    // one division
+    const double B2 = B * B;
+    F = exp_t(LN10 * lF * B2 / fma(A, A, B2), s.tab);
   } else {
     const double *c = t.sri_x + 5 * p;  // a, -b, -1/c, d, e
     const double X = 1.0 / (1.0 + lP * lP);
     const double base = c[0] * exp_t(c[1] * s.invT, s.tab) + exp_t(s.T * c[2], s.tab);
-    F = exp_t(X * log(base), s.tab);
+    F = exp_t(X * log_t(base, s.ltab), s.tab);
     if (t.pm_sri_de[p]) F *= c[3] * exp_t(c[4] * s.logT, s.tab);
   }
   return low ? F * Pr * inv1p : F * inv1p;
@@ -653,8 +666,9 @@ __global__ void __launch_bounds__(256, 1)
     const double P = b.P[i];
     s.P = P;
     s.invT = 1.0 / s.T;
-    s.logT = log(s.T);
+    s.logT = log_t(s.T, t.logtab);
     s.tab = t.exptab;
+    s.ltab = t.logtab;
     // eval_conc
     double ysum = 0.0, mwi = 0.0;
     for (int k = 0; k < N - 1; ++k) {
@@ -742,8 +756,9 @@ __global__ void __launch_bounds__(FTW * 32, 1)
     const double P = b.P[ic];
     s.P = P;
     s.invT = 1.0 / s.T;
-    s.logT = log(s.T);
+    s.logT = log_t(s.T, t.logtab);
     s.tab = t.exptab;
+    s.ltab = t.logtab;
     if (warp == 0) {
       // y_N = 1 - sum y in the reference's left-to-right order
       // (rate_subs.py:1312-1320), and the mean molecular weight
@@ -828,7 +843,7 @@ __global__ void __launch_bounds__(DW * 32)
       bT[lane] = T;
       bP[lane] = i < b.n ? b.P[i] : 101325.0;
       biT[lane] = 1.0 / T;
-      blT[lane] = log(T);
+      blT[lane] = log_t(T, t.logtab);
     }
     __syncwarp();
     const int jn = (b.n - i0) < 32 ? (int)(b.n - i0) : 32;
@@ -839,6 +854,7 @@ __global__ void __launch_bounds__(DW * 32)
       s.invT = biT[j];
       s.logT = blT[j];
       s.tab = t.exptab;
+      s.ltab = t.logtab;
       const double P = bP[j];
       s.P = P;
       // concentrations (lanes over species)

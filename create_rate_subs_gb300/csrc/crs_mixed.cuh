@@ -336,6 +336,12 @@ __device__ float pres_mod(const Tab &t, int p, const State &s, float mix,
   return low ? F * frac : F * inv1p;
 }
 
+// The stoichiometric coefficient of a compact nu-list entry: its top 16
+// bits, the rest zero (integer operations only).
+__device__ __forceinline__ double nu_of(uint16_t top) {
+  return __hiloint2double((int)((unsigned)top << 16), 0);
+}
+
 // wdot[k] += nu * net (FP64) for the reactions of one block, in order.
 template <int NNU, class DC>
 __device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
@@ -355,7 +361,7 @@ __device__ __forceinline__ void accumulate(const Tab &t, const int *rr, int cnt,
     }
 #pragma unroll
     for (int q = 0; q < NNU; ++q)
-      W[k[q]] = fma(__hiloint2double(t.nu_hi[e0 + q], 0), net[u], w[q]);  // FP64
+      W[k[q]] = fma(nu_of(t.nu_hi[e0 + q]), net[u], w[q]);  // FP64
   }
 }
 
@@ -372,7 +378,7 @@ struct WSink {
   __device__ __forceinline__ void one(const Tab &t, int r, double net) const {
     for (int e = t.nu_ptr[r]; e < t.nu_ptr[r + 1]; ++e) {
       const int k = t.nu_sp16[e];
-      W[k] = fma(__hiloint2double(t.nu_hi[e], 0), net, W[k]);  // FP64 accumulation
+      W[k] = fma(nu_of(t.nu_hi[e]), net, W[k]);  // FP64 accumulation
     }
   }
 };

@@ -336,16 +336,18 @@ __global__ void k_output(int64_t n, const float *Yh, int64_t ldy, int nsp, const
 // |dy| (|w| + s) to first order, so an error in y is the reported error
 // e = max_k |w_k - w_k,exact| / (|w_k,exact| + s_k).  The gate score of a
 // state is
-//   g = log10(D + 1e-4) + E,   D = max_k |y_k,a - y_k,b|,
+//   g = dweight log10(D + 1e-4) + E,   D = max_k |y_k,a - y_k,b|,
 // the members' disagreement plus E = est[i * lde], the output of a network
-// trained to predict log10(e + 1e-4) (omitted when est is NULL).  A state
+// trained to predict log10(e + 1e-4) (omitted when est is NULL); the
+// disagreement term is weighted by dweight (0 when the error network takes
+// D as an input, see k_disagreement).  A state
 // goes back to the exact kernel as in k_output, or when g > stol (NaN
 // included).  gate[i] (optional) receives g, for calibrating stol.
 __global__ void k_output2(int64_t n, const float *Ya, const float *Yb, int64_t ldy, int nsp,
                           const float *sm, const int *se, const float *cons, int nelem,
-                          float tol, const float *est, int64_t lde, float stol,
-                          const unsigned char *out_of_box, double *wdot, int64_t ld,
-                          unsigned char *fallback, float *gate) {
+                          float tol, float dweight, const float *est, int64_t lde,
+                          float stol, const unsigned char *out_of_box, double *wdot,
+                          int64_t ld, unsigned char *fallback, float *gate) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float sum[MAX_ELEM], mag[MAX_ELEM];
@@ -371,10 +373,23 @@ __global__ void k_output2(int64_t n, const float *Ya, const float *Yb, int64_t l
 #pragma unroll
     for (int e = 0; e < MAX_ELEM; ++e)
       if (e < nelem && mag[e] > 0.0f) worst = fmaxf(worst, fabsf(sum[e]) / mag[e]);
-    const float g = log10f(d + 1.0e-4f) + (est ? est[i * lde] : 0.0f);
+    const float g = dweight * log10f(d + 1.0e-4f) + (est ? est[i * lde] : 0.0f);
     const bool fb = !(worst <= tol) || !(g <= stol) || (out_of_box && out_of_box[i]);
     fallback[i] = fb;
     if (gate) gate[i] = g;
+  }
+}
+
+// The members' disagreement D = max_k |y_k,a - y_k,b| as an input of the
+// error network: X[i][col] = bf16((log10(D + 1e-4) - mu) / sd).
+__global__ void k_disagreement(int64_t n, const float *Ya, const float *Yb, int64_t ldy,
+                               int nsp, float mu, float sd, __nv_bfloat16 *X, int64_t ldx,
+                               int col) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float d = 0.0f;
+    for (int k = 0; k < nsp; ++k) d = fmaxf(d, fabsf(Ya[i * ldy + k] - Yb[i * ldy + k]));
+    X[i * ldx + col] = __float2bfloat16_rn((log10f(d + 1.0e-4f) - mu) / sd);
   }
 }
 
@@ -571,7 +586,7 @@ int crs_surrogate_output(int64_t n, const float *Yh, int64_t ldy, int nsp, const
 
 int crs_surrogate_output2(int64_t n, const float *Ya, const float *Yb, int64_t ldy, int nsp,
                           const float *scale_m, const int *scale_e, const float *cons, int nelem,
-                          float tol, const float *est, int64_t lde, float stol,
+                          float tol, float dweight, const float *est, int64_t lde, float stol,
                           const unsigned char *out_of_box, double *wdot, int64_t ld,
                           unsigned char *fallback, float *gate, void *stream) {
   if (n < 0 || !Ya || !Yb || !scale_m || !scale_e || !wdot || !fallback ||
@@ -580,8 +595,19 @@ int crs_surrogate_output2(int64_t n, const float *Ya, const float *Yb, int64_t l
     return bad(__func__);
   if (n == 0) return CRS_OK;
   mlp::k_output2<<<mlp::grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      n, Ya, Yb, ldy, nsp, scale_m, scale_e, cons, nelem, tol, est, lde, stol, out_of_box,
-      wdot, ld, fallback, gate);
+      n, Ya, Yb, ldy, nsp, scale_m, scale_e, cons, nelem, tol, dweight, est, lde, stol,
+      out_of_box, wdot, ld, fallback, gate);
+  return done(cudaGetLastError(), __func__);
+}
+
+int crs_surrogate_disagreement(int64_t n, const float *Ya, const float *Yb, int64_t ldy,
+                               int nsp, float mu, float sd, void *X, int64_t ldx, int col,
+                               void *stream) {
+  if (n < 0 || !Ya || !Yb || !X || ldy < nsp || col < 0 || col >= ldx || !(sd > 0.0f))
+    return bad(__func__);
+  if (n == 0) return CRS_OK;
+  mlp::k_disagreement<<<mlp::grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      n, Ya, Yb, ldy, nsp, mu, sd, static_cast<__nv_bfloat16 *>(X), ldx, col);
   return done(cudaGetLastError(), __func__);
 }
 

@@ -30,6 +30,8 @@ import numpy as np
 from . import _lib
 from .mechanism import Mechanism
 
+HOST_STAGED = 0x100   # crs_wdot_host: chunks through device buffers (CRS_HOST_STAGED)
+
 __all__ = ["RateSubs"]
 
 
@@ -240,12 +242,14 @@ class RateSubs(object):
             _ptr(o["pm"]) if self.n_pdep else None, _lib.MODES[mode], self._stream()))
         return o
 
-    def wdot_host(self, T, P, Y, mode="fp64", out=None):
-        """wdot (N, n) from host arrays, through crs_wdot_host: chunks of
-        states pass through the GPU on two streams, copies overlapping
-        kernels.  T, P: (n,), Y: (>= N-1, n) float64 numpy arrays or CPU
-        torch tensors (pinned memory lets the copies overlap); out: same
-        kinds, (N, n).  Returns out (a numpy array when allocated here)."""
+    def wdot_host(self, T, P, Y, mode="fp64", out=None, staged=False):
+        """wdot (N, n) from host arrays, through crs_wdot_host.  T, P: (n,),
+        Y: (>= N-1, n) float64 numpy arrays or CPU torch tensors; out: same
+        kinds, (N, n).  Pinned CPU tensors (all four) are read and written
+        in place by one launch over the host link; other arrays, or
+        staged=True, pass through the GPU in chunks on two streams, copies
+        overlapping kernels.  Returns out (a numpy array when allocated
+        here)."""
         torch = _torch()
 
         def host(a, name, shape0=None):
@@ -274,7 +278,8 @@ class RateSubs(object):
         with torch.cuda.device(self.device):
             _lib.check(self.lib.crs_wdot_host(self.h, n, ctypes.c_void_p(pT),
                                               ctypes.c_void_p(pP), ctypes.c_void_p(pY), ld,
-                                              ctypes.c_void_p(pW), _lib.MODES[mode]))
+                                              ctypes.c_void_p(pW),
+                                              _lib.MODES[mode] | (HOST_STAGED if staged else 0)))
         return out
 
     def status(self):

@@ -28,10 +28,12 @@ Every evaluation is gated.  A state goes back to the exact kernel
   (widened by 2 % of each feature's range), or
 * its element residual max_e |sum_k a_ek w_k| / sum_k a_ek (|w_k| + s_k)
   exceeds ``tol`` (exact production rates conserve every element), or
-* its error score g = log10(D + 1e-4) + E exceeds ``stol``: D is the
-  members' disagreement max_k |y_k,a - y_k,b|, E the output of an error
-  network (55 -> 256 -> 256 -> 1) trained on held-out states, labelled by
-  the exact kernel, to predict log10(e + 1e-4) of the served result.
+* its error score exceeds ``stol``: the output of an error network
+  (56 -> 256 -> 256 -> 1: the 55 features and the members' disagreement
+  D = max_k |y_k,a - y_k,b| as log10(D + 1e-4), standardised) trained on
+  held-out states, labelled by the exact kernel, to predict log10(e + 1e-4)
+  of the served result.  Before ``fit_gate`` the score is log10(D + 1e-4)
+  alone.
 
 ``calibrate(bound)`` sets ``stol`` from a further held-out set labelled by
 the exact kernel: the largest score up to which every calibration state
@@ -311,9 +313,14 @@ class Surrogate(object):
         self.nets = [MLP([self.n_in] + list(hidden) + [N], seed=seed + 7919 * j,
                          device=self.device) for j in range(members)]
         self.net = self.nets[0]
-        self.err_net = MLP([self.n_in] + list(err_hidden) + [1], seed=seed + 104729,
+        # the error network reads the features and, in the first padding
+        # column, the members' standardised log10 disagreement
+        self.err_net = MLP([self.n_in + 1] + list(err_hidden) + [1], seed=seed + 104729,
                            device=self.device)
+        if self.err_net.pad[0] != self.net.pad[0]:
+            raise ValueError("the feature rows need a free padding column")
         self.err_trained = False
+        self.gate_mu, self.gate_sd = 0.0, 1.0
         self.stol = float("inf")   # gate threshold on the error score
         self.bound = None          # the calibrated error bound, if any
         self.batch = int(batch)
@@ -469,10 +476,16 @@ class Surrogate(object):
             raise ValueError("number of states must be a multiple of the batch")
         Yr = Y[: self.N - 1].contiguous()
         W = self.rs.wdot(T, P, Yr, mode="fp64")
-        w, _, _ = self._serve(T, P, Yr, stol=float("inf"), use_err=False)
+        w, _, g = self._serve(T, P, Yr, stol=float("inf"), use_err=False)  # g: log10(D+1e-4)
         tgt = torch.log10(self.served_error(w, W) + 1e-4).float()[:, None].contiguous()
         del W, w
+        self.gate_mu = float(g.mean())
+        self.gate_sd = max(float(g.std()), 1e-6)
         X, XT = self._batches(T, P, Y, n)
+        v = ((g - self.gate_mu) / self.gate_sd).to(torch.bfloat16)
+        X[:, self.n_in] = v
+        XT[:, self.n_in, :] = v.view(-1, B)
+        del g, v
         losses = self._train(self.err_net, X, XT, tgt, epochs, lr, lr_final, seed)
         self.err_trained = True
         return losses
@@ -568,12 +581,16 @@ class Surrogate(object):
             net.infer(X, n, y, s)
         est = None
         if use_err and self.err_trained:
+            _lib.check(self.lib.crs_surrogate_disagreement(
+                n, _p(Yh[0]), _p(Yh[-1]), Yh[0].stride(0), N, self.gate_mu, self.gate_sd,
+                _p(X), X.stride(0), self.n_in, s))
             est = torch.empty((n, 4), **f32)
             self.err_net.infer(X, n, est, s)
         _lib.check(self.lib.crs_surrogate_output2(
             n, _p(Yh[0]), _p(Yh[-1]), Yh[0].stride(0), N, _p(self._scale_m), _p(self._scale_e),
-            _p(self._cons), self.n_elem, tol, _p(est), est.stride(0) if est is not None else 0,
-            stol, _p(box), _p(out), n, _p(flag), _p(gate), s))
+            _p(self._cons), self.n_elem, tol, 0.0 if est is not None else 1.0, _p(est),
+            est.stride(0) if est is not None else 0, stol, _p(box), _p(out), n, _p(flag),
+            _p(gate), s))
         return out, flag, gate
 
     def wdot(self, T, P, Y, tol=0.05, stol=None, out=None, with_fallback=True):
@@ -616,7 +633,7 @@ class Surrogate(object):
             d[k] = getattr(self, k).cpu().numpy()
         d["history"] = np.array(self.history)
         d["gate"] = np.array([self.stol, np.nan if self.bound is None else self.bound,
-                              float(self.err_trained)])
+                              float(self.err_trained), self.gate_mu, self.gate_sd])
         np.savez(path, **d)
 
     def load(self, path):
@@ -630,6 +647,6 @@ class Surrogate(object):
             getattr(self, k).copy_(torch.from_numpy(d[k]))
         self.set_scale(d["scale"])
         self.history = list(d.get("history", []))
-        stol, bound, trained = (float(x) for x in d["gate"])
+        stol, bound, trained, self.gate_mu, self.gate_sd = (float(x) for x in d["gate"])
         self.stol, self.bound = stol, (None if math.isnan(bound) else bound)
         self.err_trained = bool(trained)

@@ -55,7 +55,7 @@ typedef struct crs_mech crs_mech;
  * layout: one state per thread (TPS) or one state per warp (WARP).  The
  * default modes pick the faster layout that fits the mechanism.
  * CRS_MODE_MIXED_TPS also needs every stoichiometric coefficient to be
- * exact in 21 significant bits (integers, halves, ...); else, like a
+ * exact in 5 significant bits (integers up to 31, halves, ...); else, like a
  * mechanism whose per-thread columns do not fit, it returns
  * CRS_ERR_UNSUPPORTED and CRS_MODE_MIXED runs the warp layout. */
 #define CRS_MODE_FP64_TPS 3
@@ -173,12 +173,17 @@ int crs_dydt(const crs_mech *mech, int64_t n, const double *p_or_rho,
 
 /* wdot from HOST arrays (same SoA layout and ld as crs_wdot): the batched
  * form of the reference's per-state host functions (rate_subs.py:1297-1299,
- * 287-290, 761-763, 1124-1127 evaluated for every state).  States go
- * through the device in chunks on two streams owned by the handle, so that
- * the copies of one chunk overlap the kernel of the other; pinned
- * (page-locked) host memory is needed for that overlap.  Returns when wdot
- * is on the host.  Device buffers (<= 2 x 256 MB) are allocated on first
- * use and kept by the handle; calls on one handle are serialised. */
+ * 287-290, 761-763, 1124-1127 evaluated for every state).  When all four
+ * arrays are page-locked host memory that the current device can address
+ * (cudaHostAlloc, torch's pin_memory, cudaHostRegister), one launch reads
+ * the states and writes wdot in place over the host link (NVLink-C2C on
+ * Grace).  Otherwise, or with CRS_HOST_STAGED or'ed into `mode`, states go
+ * through device buffers in chunks on two streams owned by the handle, so
+ * that the copies of one chunk overlap the kernel of the other (pinned
+ * memory is needed for that overlap; the buffers, <= 2 x 256 MB, are
+ * allocated on first use and kept by the handle).  Returns when wdot is on
+ * the host; calls on one handle are serialised. */
+#define CRS_HOST_STAGED 0x100
 int crs_wdot_host(const crs_mech *mech, int64_t n, const double *T,
                   const double *P, const double *Y, int64_t ld,
                   double *wdot, int mode);
@@ -307,18 +312,25 @@ int crs_surrogate_output(int64_t n, const float *Yh, int64_t ldy, int nsp,
 /* Two-network form of crs_surrogate_output with an error gate (no
  * counterpart in the reference).  Ya and Yb are two networks' outputs
  * (same layout); the served y is their mean.  Gate score of state i:
- * g = log10(D + 1e-4) + est[i * lde], D = max_k |Ya[i][k] - Yb[i][k]| (the
- * networks' disagreement) and est the output of an error network trained
- * to predict log10 of the served error + 1e-4 (may be NULL: term omitted).
- * fallback[i] = 1 as in crs_surrogate_output, or when g > stol (NaN
- * included).  gate (may be NULL) receives g. */
+ * g = dweight log10(D + 1e-4) + est[i * lde], D = max_k |Ya[i][k] -
+ * Yb[i][k]| (the networks' disagreement) and est the output of an error
+ * network trained to predict log10 of the served error + 1e-4 (may be NULL:
+ * term omitted).  fallback[i] = 1 as in crs_surrogate_output, or when
+ * g > stol (NaN included).  gate (may be NULL) receives g. */
 int crs_surrogate_output2(int64_t n, const float *Ya, const float *Yb,
                           int64_t ldy, int nsp, const float *scale_m,
                           const int *scale_e, const float *cons, int nelem,
-                          float tol, const float *est, int64_t lde, float stol,
+                          float tol, float dweight, const float *est,
+                          int64_t lde, float stol,
                           const unsigned char *out_of_box, double *wdot,
                           int64_t ld, unsigned char *fallback, float *gate,
                           void *stream);
+/* The networks' disagreement as an input of the error network (no
+ * counterpart in the reference): X[i * ldx + col] (bf16 feature rows) =
+ * (log10(D + 1e-4) - mu) / sd, D as in crs_surrogate_output2. */
+int crs_surrogate_disagreement(int64_t n, const float *Ya, const float *Yb,
+                               int64_t ldy, int nsp, float mu, float sd,
+                               void *X, int64_t ldx, int col, void *stream);
 /* idx[0..count) = the i < n with flag[i] != 0, in no particular order
  * (count: device int64, set by the call). */
 int crs_select(int64_t n, const unsigned char *flag, int64_t *idx,

@@ -51,8 +51,9 @@ struct ImgLayout {
   // derived f64 sections (fast kernels): per rate row (logA, b, -Ta); per
   // reversible reaction log(Kc prefactor); per pres_mod entry the Troe and
   // SRI constants in multiply form; per species the 2x7 Gibbs
-  // coefficients; the 256-entry 2^(j/256) table of the exponential.
-  int rate_x, kc_lpref, troe_x, sri_x, sp_gibbs, exptab;
+  // coefficients; the 256-entry 2^(j/256) table of the exponential; the
+  // 129 pairs (1/F, log F), F = 1 + j/128, of the logarithm.
+  int rate_x, kc_lpref, troe_x, sri_x, sp_gibbs, exptab, logtab;
   // derived f32 sections (mixed kernel): per rate row ln|A|, b, -Ta as
   // float-float pairs and sign(A); 1/mw; Troe and SRI constants (exponent
   // factors as float-float pairs); efficiencies minus one.
@@ -63,8 +64,8 @@ struct ImgLayout {
   // reaction has a single T_common group (kc_single = 1)
   int kc_poly, kc_single;
   // derived sections (mixed, one state per thread): the net-nu species as
-  // int16 and each nu as the high word of its double (nu_hi_exact = 1 when
-  // every nu's low word is zero, i.e. the pair is exact)
+  // int16 and each nu as the top 16 bits of its double (nu_hi_exact = 1 when
+  // every nu's other 48 bits are zero, i.e. the pair is exact)
   int nu_sp16, nu_hi, nu_hi_exact;
   // derived f64 section (thermo utilities): per species 24 doubles
   // [RU/mw, mw, T_common, 0, lo: a0..a5, a1/2, a2/3, a3/4, a4/5, hi: same]
@@ -97,10 +98,11 @@ struct Tab {
   const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
   const double *spc_nu;
   const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
-  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *kc_poly, *sp_thermo;
+  const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *logtab, *kc_poly,
+      *sp_thermo;
   int kc_single;
   const int16_t *nu_sp16;
-  const int32_t *nu_hi;
+  const uint16_t *nu_hi;
   const double *inv_mw, *rate_par, *rx_nu, *px_nu, *kc_tmid, *kc_lo, *kc_hi,
       *kc_pref, *pm_eff_val, *pm_troe, *pm_sri, *nu_val, *sp_tmid, *sp_lo,
       *sp_hi, *kc_dnu, *sp_mw;
@@ -129,12 +131,12 @@ CRS_HD inline Tab make_tab2(const unsigned char *near,
 #define CRS_S(x) t.x = reinterpret_cast<const float *>(CRS_P(x))
 #define CRS_I(x) t.x = reinterpret_cast<const int32_t *>(CRS_P(x))
   CRS_F(rate_x); CRS_F(kc_lpref); CRS_F(troe_x); CRS_F(sri_x); CRS_F(sp_gibbs);
-  CRS_F(exptab); CRS_F(kc_poly); CRS_F(sp_thermo);
+  CRS_F(exptab); CRS_F(logtab); CRS_F(kc_poly); CRS_F(sp_thermo);
   CRS_I(perm); CRS_I(seg);
   t.rfac = reinterpret_cast<const int16_t *>(CRS_P(rfac));
   t.pfac = reinterpret_cast<const int16_t *>(CRS_P(pfac));
   t.nu_sp16 = reinterpret_cast<const int16_t *>(CRS_P(nu_sp16));
-  CRS_I(nu_hi);
+  t.nu_hi = reinterpret_cast<const uint16_t *>(CRS_P(nu_hi));
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
   CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
