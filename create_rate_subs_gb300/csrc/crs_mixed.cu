@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(352, 1)
     // once to FP32
     double ysum = 0.0, mwi = 0.0;
     for (int k = 0; k < N - 1; ++k) {
-      const double y = b.Y[(int64_t)k * b.ld + i];
+      // streamed: read once, evict first, so that L1 keeps the rate rows
+      const double y = __ldcs(b.Y + (int64_t)k * b.ld + i);
       ysum += y;
       mwi = fma(y, t.inv_mw[k], mwi);
       W[k] = y;  // parked in the accumulator column until C is formed
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(352, 1)
     for (int k = 0; k < N; ++k) {
       const double v = W[k];
       bad += ((__double2hiint(v) >> 20) & 0x7ff) == 0x7ff;  // inf or NaN, integer test
-      b.wdot[(int64_t)k * b.ld + i] = v;
+      __stcs(b.wdot + (int64_t)k * b.ld + i, v);  // streamed out
     }
   }
   if (bad && b.status) atomicAdd(&b.status[1], bad);

@@ -44,7 +44,8 @@ struct ImgLayout {
   // shared memory (two ranges per kernel, copied back to back); sections
   // outside them are read from global memory through L1.
   //   [0] FP64 one state per thread   [1] FP64 one state per warp
-  //   [2] mixed one state per thread, Kc polynomials read through L1
+  //   [2] mixed one state per thread, Kc polynomials and rate rows read
+  //       through L1
   //   [3] mixed one state per warp
   //   [4] mixed one state per thread, Kc polynomials in shared memory
   int rng[5][4];
