@@ -56,7 +56,7 @@ def _args():
                     help="fresh states the surrogate is evaluated on")
     ap.add_argument("--sur-bound", type=float, default=0.1,
                     help="error bound the surrogate's gate is calibrated for")
-    ap.add_argument("--sur-gate-states", type=int, default=1 << 23,
+    ap.add_argument("--sur-gate-states", type=int, default=1 << 24,
                     help="held-out states the error network is trained on")
     ap.add_argument("--sur-cal-states", type=int, default=1 << 24,
                     help="held-out states the gate threshold is calibrated on")

@@ -337,6 +337,8 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
     return fail(CRS_ERR_BLOB, "could not derive fast tables");
   L.kc_single = 1;
   for (int j = 0; j < L.NREV; ++j) L.kc_single &= (t.kc_ptr[j + 1] - t.kc_ptr[j]) <= 1;
+  L.nw = 0;
+  for (int e = 0; e < t.nu_ptr[L.R]; ++e) L.nw = std::max(L.nw, (int)t.nu_sp[e] + 1);
   L.nu_hi_exact = 1;
   for (int e = 0; e < t.nu_ptr[L.R]; ++e) {
     uint64_t u;

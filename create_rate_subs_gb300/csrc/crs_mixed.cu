@@ -27,13 +27,15 @@
 
 #include <cuda_bf16.h>
 
+#include "crs_exp.cuh"
 #include "crs_mixed.cuh"
 
 namespace crs {
 namespace mixed {
 
 // One state per thread.  Per-state shared-memory columns: C (fp32) and
-// the wdot accumulators W (FP64), 12 B per species and thread; the Kc
+// the wdot accumulators W (FP64; only for the species below L.nw, the
+// others never accumulate), 12 B per species and thread; the Kc
 // exponents come from the per-reaction polynomials (no Gibbs column, the
 // polynomials read through L1), and only the tables of this kernel's hot
 // loop are staged, so that ~300 threads fit.  KC1: one T_common group per
@@ -51,11 +53,11 @@ __global__ void __launch_bounds__(352, 1)
     sched_done(b.sched, amask, lane);
     return;
   }
-  const int N = t.N;
+  const int N = t.N, NW = L.nw;
   const int st = blockDim.x;
   double *dbase = reinterpret_cast<double *>(smem + nb);
   const DCol W{dbase + threadIdx.x, st};
-  const FCol C{reinterpret_cast<float *>(dbase + N * st) + threadIdx.x, st};
+  const FCol C{reinterpret_cast<float *>(dbase + NW * st) + threadIdx.x, st};
   int bad = 0;
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - (int64_t)gridDim.x * blockDim.x;
   for (;;) {
@@ -72,11 +74,11 @@ __global__ void __launch_bounds__(352, 1)
     const double P = b.P[i];
     s.P = P;
     s.invT = 1.0 / s.T;
-    s.logT = log(s.T);
+    s.logT = texp::log_t(s.T, t.logtab);  // table logarithm (12 FP64 instructions)
     s.Tf = (float)s.T;
-    s.Tff = ff_from_double(s.T);
-    s.lTff = ff_from_double(s.logT);
-    s.iTff = ff_from_double(s.invT);
+    s.Tff = ff_from_double_int(s.T);  // splits by integer operations
+    s.lTff = ff_from_double_int(s.logT);
+    s.iTff = ff_from_double_int(s.invT);
     // concentrations: sums and C = y * (rho / mw) in FP64, each C rounded
     // once to FP32
     double ysum = 0.0, mwi = 0.0;
@@ -85,17 +87,18 @@ __global__ void __launch_bounds__(352, 1)
       const double y = __ldcs(b.Y + (int64_t)k * b.ld + i);
       ysum += y;
       mwi = fma(y, t.inv_mw[k], mwi);
-      W[k] = y;  // parked in the accumulator column until C is formed
+      if (k < NW) W[k] = y;  // parked in the accumulator column until C is formed
     }
     const double yN = 1.0 - ysum;
     mwi = fma(yN, t.inv_mw[N - 1], mwi);
     const double rho = P / mwi * (s.invT * INV_RU);
     for (int k = 0; k < N - 1; ++k) {
-      C[k] = d2f_rn(W[k] * (rho * t.inv_mw[k]));
-      W[k] = 0.0;
+      const double y = k < NW ? W[k] : b.Y[(int64_t)k * b.ld + i];  // no column: read again
+      C[k] = d2f_rn(y * (rho * t.inv_mw[k]));
+      if (k < NW) W[k] = 0.0;
     }
     C[N - 1] = d2f_rn(yN * (rho * t.inv_mw[N - 1]));
-    W[N - 1] = 0.0;
+    if (N - 1 < NW) W[N - 1] = 0.0;
     if (STAGES && b.conc)
       for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = (double)C[k];
     const float mix = d2f_rn(P * s.invT * INV_RU);
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(352, 1)
     for (int p = t.seg[NSHAPE + 1]; p < t.R; ++p)  // PLOG / Chebyshev
       general<STAGES, true>(t, t.perm[p], s, mix, C, kc, sink, b, i);
     for (int k = 0; k < N; ++k) {
-      const double v = W[k];
+      const double v = k < NW ? W[k] : 0.0;
       bad += ((__double2hiint(v) >> 20) & 0x7ff) == 0x7ff;  // inf or NaN, integer test
       __stcs(b.wdot + (int64_t)k * b.ld + i, v);  // streamed out
     }
@@ -314,7 +317,7 @@ cudaError_t launch_wdot_mixed_tps(const unsigned char *img, const ImgLayout &L,
   auto k = L.kc_single ? (stages ? mixed::k_wdot<true, true> : mixed::k_wdot<false, true>)
                        : (stages ? mixed::k_wdot<true, false> : mixed::k_wdot<false, false>);
   const size_t tab = (size_t)(L.rng[2][1] - L.rng[2][0] + L.rng[2][3] - L.rng[2][2]);
-  const size_t per = (size_t)L.N * (8 + 4);
+  const size_t per = (size_t)L.nw * 8 + (size_t)L.N * 4;
   const long long room = (long long)smem_optin - (long long)tab;
   // any thread count, but a last warp under half full is dropped: the FP64
   // pipe charges a whole warp instruction whatever the active lanes, so a

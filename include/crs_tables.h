@@ -68,6 +68,9 @@ struct ImgLayout {
   // int16 and each nu as the top 16 bits of its double (nu_hi_exact = 1 when
   // every nu's other 48 bits are zero, i.e. the pair is exact)
   int nu_sp16, nu_hi, nu_hi_exact;
+  // 1 + the highest species index with a nonzero net nu: species at or
+  // above it (bath gases listed last) never accumulate a rate
+  int nw;
   // derived f64 section (thermo utilities): per species 24 doubles
   // [RU/mw, mw, T_common, 0, lo: a0..a5, a1/2, a2/3, a3/4, a4/5, hi: same]
   int sp_thermo;
