@@ -255,18 +255,3 @@ def test_gated_surrogate_bounds_error_and_beats_plain_fp64(rs, gated):
     assert 0 < nfb < n
     assert float(err.max()) <= GAIN_BOUND
     assert ms_sur < ms_plain
-
-
-def test_gate_threshold_is_the_last_clean_score():
-    """threshold(): the largest score below the first state over the bound,
-    ties with that state excluded."""
-    from create_rate_subs_gb300.surrogate import Surrogate
-    g = torch.tensor([0.1, 0.5, 0.3, 0.9, 0.7], device="cuda")
-    e = torch.tensor([0.0, 0.0, 0.0, 1.0, 0.0], device="cuda")
-    assert Surrogate.threshold(g, e, 0.5) == pytest.approx(0.7)
-    e[0] = 1.0
-    assert Surrogate.threshold(g, e, 0.5) == float("-inf")
-    g2 = torch.tensor([0.1, 0.3, 0.3], device="cuda")
-    e2 = torch.tensor([0.0, 0.0, 1.0], device="cuda")
-    assert Surrogate.threshold(g2, e2, 0.5) == pytest.approx(0.1)
-    assert Surrogate.threshold(g2, torch.zeros(3, device="cuda"), 0.5) == pytest.approx(0.3)
