@@ -382,8 +382,13 @@ def run_ours(args):
     rs = RateSubs(mech)
     lib = _lib.load()
     N = mech.n_species
-    n = args.states
-    T, P, Y = synth.make_states(N, n, seed=1000 + rank)
+    # weak scaling: the job is one seeded batch of world x --states states;
+    # each rank evaluates its slab of it (shard.shard_range), drawn from the
+    # slab's own seed, with no collective on the data path
+    from create_rate_subs_gb300.shard import shard_range
+    a, b_ = shard_range(world * args.states, rank, world)
+    n = b_ - a
+    T, P, Y = synth.make_states(N, n, seed=1000 + a)
     dT, dP, dY = (torch.from_numpy(a).cuda() for a in (T, P, Y[: N - 1].copy()))
     out = torch.empty((N, n), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
