@@ -39,14 +39,17 @@ namespace large {
 
 using namespace mixed;
 
-constexpr int TW = 4;        // warps per CTA of the rates kernel
+// warps per CTA of the rates kernel: two CTAs of 8 warps fit an SM (two
+// 72 KB concentration tiles at 561 species, 128 registers per thread), 16
+// warps against 12 with three CTAs of 4 (+15% for the mixed rates pass)
+constexpr int TW = 8;
 constexpr int WINDOW = 100;  // binary orders around c_s carried by bf16 hi + lo
 
 using tile::QSink;
 using tile::RatesOut;
 
 template <bool KC1>
-__global__ void __launch_bounds__(TW * 32, 3)
+__global__ void __launch_bounds__(TW * 32, 2)
     k_rates_tile(const unsigned char *__restrict__ img, ImgLayout L, Batch b, RatesOut o) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ double s_rho[32], s_yN[32];
