@@ -731,7 +731,10 @@ __global__ void __launch_bounds__(256, 1)
 // 256 B per species), FTW warps taking the shape blocks round-robin, every
 // net rate written to HBM for the species sums.  For mechanisms whose
 // per-thread columns do not fit on chip.
-constexpr int FTW = 12;  // 12 warps at 168 registers (8: 4.59, 12: 4.81, 16: 4.76 M states/s at 561/2539)
+// 12 warps at 168 registers (8: 4.59, 12: 4.81, 16: 4.76 M states/s at 561/2539;
+// 4.90 at 12 with the state sums on two warps)
+constexpr int FTW = 12;
+static_assert(FTW >= 2, "tile::state_sums runs on warps 0 and 1");
 
 template <bool KC1>
 __global__ void __launch_bounds__(FTW * 32, 1)
@@ -759,17 +762,7 @@ __global__ void __launch_bounds__(FTW * 32, 1)
     s.logT = log_t(s.T, t.logtab);
     s.tab = t.exptab;
     s.ltab = t.logtab;
-    if (warp == 0) {
-      // y_N = 1 - sum y in the reference's left-to-right order
-      // (rate_subs.py:1312-1320), and the mean molecular weight
-      double ys = N > 1 ? b.Y[ic] : 0.0, mwi = 0.0;
-      for (int k = 1; k < N - 1; ++k) ys += b.Y[(int64_t)k * b.ld + ic];
-      const double yN = 1.0 - ys;
-      for (int k = 0; k < N - 1; ++k) mwi = fma(b.Y[(int64_t)k * b.ld + ic], t.inv_mw[k], mwi);
-      mwi = fma(yN, t.inv_mw[N - 1], mwi);
-      s_rho[lane] = P / mwi * (s.invT * INV_RU);
-      s_yN[lane] = yN;
-    }
+    tile::state_sums(t, b, ic, warp, lane, P, s.invT * INV_RU, s_yN, s_rho);
     __syncthreads();
     const double rho = s_rho[lane];
     for (int k = warp; k < N; k += FTW) {

@@ -43,6 +43,7 @@ using namespace mixed;
 // 72 KB concentration tiles at 561 species, 128 registers per thread), 16
 // warps against 12 with three CTAs of 4 (+15% for the mixed rates pass)
 constexpr int TW = 8;
+static_assert(TW >= 2, "tile::state_sums runs on warps 0 and 1");
 constexpr int WINDOW = 100;  // binary orders around c_s carried by bf16 hi + lo
 
 using tile::QSink;
@@ -77,17 +78,7 @@ __global__ void __launch_bounds__(TW * 32, 2)
     s.Tff = ff_from_double(s.T);
     s.lTff = ff_from_double(s.logT);
     s.iTff = ff_from_double(s.invT);
-    if (warp == 0) {
-      // y_N = 1 - sum y in the reference's left-to-right order
-      // (rate_subs.py:1312-1320), and the mean molecular weight
-      double ys = N > 1 ? b.Y[ic] : 0.0, mwi = 0.0;
-      for (int k = 1; k < N - 1; ++k) ys += b.Y[(int64_t)k * b.ld + ic];
-      const double yN = 1.0 - ys;
-      for (int k = 0; k < N - 1; ++k) mwi = fma(b.Y[(int64_t)k * b.ld + ic], t.inv_mw[k], mwi);
-      mwi = fma(yN, t.inv_mw[N - 1], mwi);
-      s_rho[lane] = P / mwi * (s.invT * INV_RU);
-      s_yN[lane] = yN;
-    }
+    tile::state_sums(t, b, ic, warp, lane, P, s.invT * INV_RU, s_yN, s_rho);
     __syncthreads();
     const double rho = s_rho[lane];
     for (int k = warp; k < N; k += TW) {

@@ -71,5 +71,32 @@ __device__ __forceinline__ int scale_exponent(int es, int ec) {
   return es < 0 ? -c : c;
 }
 
+// The tile's per-state sums (lane = state, ic its column): warp 0 forms
+// y_N = 1 - the sum of the first N-1 mass fractions in the reference's
+// left-to-right order (rate_subs.py:1312-1320) into s_yN; warp 1 the sum of
+// y_k / W_k over the first N-1 species and, once y_N is known, the density
+// P / (that sum + y_N / W_N) * scale into s_rho.  The two dependent FP64
+// chains (N-2 additions, N-1 FMAs) run side by side on two warps, with the
+// operations and their order of one warp doing both; the two warps meet at
+// named barrier 1, and the caller's __syncthreads publishes the results
+// to the other warps.  Needs a CTA of two or more warps.
+__device__ __forceinline__ void state_sums(const Tab &t, const Batch &b, int64_t ic, int warp,
+                                           int lane, double P, double scale, double *s_yN,
+                                           double *s_rho) {
+  const int N = t.N;
+  if (warp == 0) {
+    double ys = N > 1 ? b.Y[ic] : 0.0;
+    for (int k = 1; k < N - 1; ++k) ys += b.Y[(int64_t)k * b.ld + ic];
+    s_yN[lane] = 1.0 - ys;
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+  } else if (warp == 1) {
+    double mwi = 0.0;
+    for (int k = 0; k < N - 1; ++k) mwi = fma(b.Y[(int64_t)k * b.ld + ic], t.inv_mw[k], mwi);
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    mwi = fma(s_yN[lane], t.inv_mw[N - 1], mwi);
+    s_rho[lane] = P / mwi * scale;
+  }
+}
+
 }  // namespace tile
 }  // namespace crs
