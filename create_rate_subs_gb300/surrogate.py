@@ -37,7 +37,7 @@ Every evaluation is gated.  A state goes back to the exact kernel
 
 ``calibrate(bound)`` sets ``stol`` from a further held-out set labelled by
 the exact kernel: the largest score up to which every calibration state
-has e <= margin * bound (margin 0.5 by default).  The plain kernel is thus both the fallback and the judge
+has e <= margin * bound (margin 0.5 by default).  The plain kernel is thus both the fallback and the arbiter
 of the surrogate's error; the bound holds on the calibration states and is
 measured again on fresh states by the tests and bench.py.
 
@@ -293,7 +293,7 @@ def surrogate_error(w, w_exact, scale):
 class Surrogate(object):
     """wdot(T, P, Y) from the trained networks, with gated exact fallback.
 
-    ``rs`` is a RateSubs (the exact kernel: labels, fallback and judge).
+    ``rs`` is a RateSubs (the exact kernel: labels, fallback and arbiter).
     ``members``: 2 (served y = mean of two networks, their disagreement in
     the gate) or 1."""
 
