@@ -746,7 +746,7 @@ def _bench_large(args, stream, dist, world, peaks, rank):
     sub = 4096
     steps = max(5, args.steps // 2)
     got = {}
-    precision = {"fp64": "fp64", "mixed": "mixed", "gemm": "rates"}
+    precision = {"fp64": "fp64", "mixed": "mixed_tile", "gemm": "rates"}
     for mode in ("fp64", "mixed", "gemm"):
         ms = _time_steps(lambda: rs.wdot(dT, dP, dY, mode, out=out), steps, 3, stream, dist)
         got[mode] = rs.wdot(dT[:sub], dP[:sub], dY[:, :sub], mode).cpu().numpy()

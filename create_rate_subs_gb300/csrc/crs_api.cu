@@ -419,6 +419,10 @@ int build_image(const unsigned char *b, size_t n, crs_mech *m) {
   raw(&IL::plog_p, "plog_p"); raw(&IL::plog_lp, "plog_lp"); raw(&IL::plog_dlp, "plog_dlp");
   raw(&IL::cheb_ptr, "cheb_ptr"); raw(&IL::cheb_nt, "cheb_nt"); raw(&IL::cheb_np, "cheb_np");
   raw(&IL::cheb_par, "cheb_par"); raw(&IL::cheb_tp, "cheb_tp");
+  // last: the mixed kernels' float-float Kc polynomials (read through L1).
+  // Every other section keeps the offset it has without them, and the
+  // strict kernel stages only the bytes before them (ImgLayout::kc_mix)
+  der(&IL::kc_mix);
   // every blob section and every derived table must have been placed
   for (auto &w : want) {
     bool found = false;
@@ -825,7 +829,7 @@ int crs_mech_inspect(const void *blob, size_t nbytes, int64_t out[6]) {
   out[2] = span(3);
   out[3] = span(1) + 8 * 8 * (128 + 2 * N + R + 1);          // CRS_MODE_FP64 per CTA
   out[4] = span(3) + 8 * 8 * (128 + N + R + (N + 1) / 2 + 1);  // CRS_MODE_MIXED per CTA
-  out[5] = out[0] + 2 * N * block * 8;   // CRS_MODE_FP64_STRICT, all on chip
+  out[5] = m.L.kc_mix + 2 * N * block * 8;   // CRS_MODE_FP64_STRICT, all on chip
   return CRS_OK;
 }
 

@@ -184,6 +184,22 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
   const int ne = t.pm_eff_ptr[L.NPM];
   std::vector<float> ef(ne > 0 ? ne : 1, 0.0f);
   for (int e = 0; e < ne; ++e) ef[e] = (float)t.pm_eff_val[e];
+  // the Kc polynomials (kc_poly, prefactor folded into c0) as float-float
+  // pairs for the mixed kernels, -c6 stored so that every Horner step is a
+  // multiply-add; T_common kept as a double for the same bit-pattern test
+  std::vector<float> km(32 * (size_t)(single && L.NREV > 0 ? L.NREV : 1), 0.0f);
+  if (single) {
+    for (int j = 0; j < L.NREV; ++j) {
+      for (int h = 0; h < 2; ++h) {
+        const double *c = kp.data() + 16 * j + 2 + 7 * h;
+        float *o = km.data() + 32 * j + 16 * h;
+        for (int q = 0; q < 6; ++q) split(c[q], &o[2 * q], &o[2 * q + 1]);
+        split(-c[6], &o[12], &o[13]);
+        memcpy(o + 14, kp.data() + 16 * j, sizeof(double));
+      }
+    }
+  }
+  put(extra, &ImgLayout::kc_mix, km);
   put(extra, &ImgLayout::rate_ff, rf);
   put(extra, &ImgLayout::inv_mw_f, imf);
   put(extra, &ImgLayout::troe_ff, tf);

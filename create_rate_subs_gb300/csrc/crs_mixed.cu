@@ -1,8 +1,6 @@
 // CRS_MODE_MIXED: FP32 bulk arithmetic, FP64 where stability needs it.
 //
 // FP64 instructions are kept for
-//   * the per-species Gibbs terms S_k and, per reaction, the exponent of
-//     the equilibrium constant sum_k nu_k S_k + ln(prefactor);
 //   * the net rate fwd - rev (cancels near equilibrium);
 //   * the accumulation of wdot;
 //   * per-state scalars (1/T, ln T, the mass-fraction sums behind rho).
@@ -18,7 +16,14 @@
 //     rates far outside the FP32 range (1/Kc can reach e^150 with random
 //     thermochemistry) neither overflow nor underflow; the FP64 value is
 //     assembled with integer operations only;
-//   * concentrations, third-body sums and fall-off broadening in FP32.
+//   * concentrations, third-body sums and fall-off broadening in FP32;
+//   * the exponent of the equilibrium constant, ln(prefactor) + the
+//     reaction's Kc polynomial in T, ln T and 1/T, as float-float multiply-
+//     adds (KcMix: within ~3e-12 of the FP64 polynomial for exponents up to
+//     ~400, where the FP32 rates notice 1e-7).  The warp-per-state kernel,
+//     the large mechanisms' state tile (crs_large.cu) and mechanisms with
+//     several T_common groups per reaction form it in FP64 (per-species
+//     Gibbs terms S_k, or the polynomials).
 // The error against FP64, scaled by the gross rate of each species, is
 // measured by the tests and reported by bench.py.
 #include <cuda_runtime.h>
@@ -39,7 +44,7 @@ namespace mixed {
 // exponents come from the per-reaction polynomials (no Gibbs column, the
 // polynomials read through L1), and only the tables of this kernel's hot
 // loop are staged, so that ~300 threads fit.  KC1: one T_common group per
-// reaction (kc_poly).
+// reaction (float-float polynomials, kc_mix).
 template <bool STAGES, bool KC1>
 __global__ void __launch_bounds__(352, 1)
     k_wdot(const unsigned char *__restrict__ img, ImgLayout L, Batch b) {
@@ -102,12 +107,18 @@ __global__ void __launch_bounds__(352, 1)
     if (STAGES && b.conc)
       for (int k = 0; k < N; ++k) b.conc[(int64_t)k * b.ld + i] = (double)C[k];
     const float mix = d2f_rn(P * s.invT * INV_RU);
-    using KC = typename std::conditional<KC1, KcPoly1, KcPolyG>::type;
+    using KC = typename std::conditional<KC1, KcMix, KcPolyG>::type;
     KC kc;
-    kc.T = s.T;
-    kc.logT = s.logT;
-    kc.invT = s.invT;
-    if constexpr (KC1) kc.Tbits = __double_as_longlong(s.T);
+    if constexpr (KC1) {
+      kc.Tbits = __double_as_longlong(s.T);
+      kc.T = s.Tff;
+      kc.logT = s.lTff;
+      kc.invT = s.iTff;
+    } else {
+      kc.T = s.T;
+      kc.logT = s.logT;
+      kc.invT = s.invT;
+    }
     const WSink<DCol> sink{W};
     Shapes<0, STAGES, KC, WSink<DCol>>::run(t, s, C, kc, sink, b, i);
     for (int p = t.seg[NSHAPE]; p < t.seg[NSHAPE + 1]; ++p)

@@ -219,6 +219,70 @@ struct KcFromGibbs {
   }
 };
 
+// a * b + c in float-float: the FP32 product with its FMA residuals, the
+// head of c added exactly (TwoSum, by operations that are never contracted
+// into an FMA) and every low-order term added once.  The result is left
+// unnormalised (its low part may exceed half an ulp of the head), which a
+// following ff_fma or ff_add takes as it is.  Error about 2^-44 of
+// |a b| + |c|.
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = __fadd_rn(p, c.h);
+  const float bb = __fsub_rn(s, p);
+  const float err = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(c.h, bb));
+  return ff{s, __fadd_rn(err, __fadd_rn(e, c.l))};
+}
+
+// Exponent of the equilibrium constant of reversible reaction j (with ln
+// of its prefactor) as float-float, entirely on the FP32 pipe, for the
+// mixed kernels when every reaction has a single T_common group: the
+// polynomial of KcPoly1 in the same Horner order,
+//   c0 + c1 ln T + T (c2 + T (c3 + T (c4 + c5 T))) - c6 / T,
+// with float-float coefficients (kc_mix) and float-float T, ln T and 1/T.
+// Seven multiply-adds of ~2^-44 relative error: an absolute error near
+// 1e-11 for exponents of a few hundred, against FP32 rates that notice
+// 1e-7; the FP64 pipe, which retires 1/64 of the FP32 pipe's operations on
+// GB300, does none of it.
+struct KcMix {
+  long long Tbits;  // T's bit pattern: T <= T_common as an integer test
+  ff T, logT, invT;
+};
+__device__ __forceinline__ ff kc_exponent(const KcMix &kc, const Tab &t, int, int j) {
+  const float4 *p = reinterpret_cast<const float4 *>(t.kc_mix + 32 * j);
+  const float4 lo3 = p[3];  // -c6 of the low block and T_common
+  const long long tc =
+      (long long)(((unsigned long long)__float_as_uint(lo3.w) << 32) | __float_as_uint(lo3.z));
+  const float4 *c = kc.Tbits <= tc ? p : p + 4;
+  const float4 a = c[0], b = c[1], d = c[2], e = c[3];
+  ff v = ff{d.z, d.w};                      // c5
+  v = ff_fma(v, kc.T, ff{d.x, d.y});        // c4
+  v = ff_fma(v, kc.T, ff{b.z, b.w});        // c3
+  v = ff_fma(v, kc.T, ff{b.x, b.y});        // c2
+  v = ff_fma(v, kc.T, ff{a.x, a.y});        // c0
+  v = ff_fma(ff{a.z, a.w}, kc.logT, v);     // c1 ln T
+  return ff_fma(ff{e.x, e.y}, kc.invT, v);  // -c6 / T
+}
+// Any other form (FP64 polynomials, Gibbs columns): its FP64 exponent,
+// kept as a double until the exponential needs it (kc_ff), so that the
+// FP64 chain overlaps the forward-rate work in between.
+template <class KC>
+__device__ __forceinline__ double kc_exponent(const KC &kc, const Tab &t, int r, int j) {
+  return kc(t, r, j);
+}
+template <class KC>
+struct KcOut {
+  using type = double;
+};
+template <>
+struct KcOut<KcMix> {
+  using type = ff;
+};
+__device__ __forceinline__ ff kc_ff(ff g) { return g; }
+__device__ __forceinline__ ff kc_ff(double g) { return ff_from_double_int(g); }
+
 // product of concentration factors as mantissa * 2^E
 // Product of concentration factors, times the mantissa m0 of the rate
 // constant, as mantissa * 2^E; the FP32 rounding of every multiply is kept
@@ -389,13 +453,12 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
                                             const FCol &C, const KC &kc,
                                             const SINK &sink, const Batch &b,
                                             int64_t i) {
-  // FP64 Kc exponents first: independent of the FP32 work below, so the
-  // scheduler can overlap the slow FP64 pipe with it (the block is
-  // straight-line code)
-  double g[4];
+  // Kc exponents first: independent of the rate work below, so the
+  // scheduler can overlap them with it (the block is straight-line code)
+  typename KcOut<KC>::type g[4];
   if (REV) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) g[u] = kc(t, rr[u], t.rev_idx[rr[u]]);
+    for (int u = 0; u < 4; ++u) g[u] = kc_exponent(kc, t, rr[u], t.rev_idx[rr[u]]);
   }
   ff x[4];
   double fwd[4], rev[4];
@@ -423,7 +486,7 @@ __device__ __forceinline__ void shape_block(const Tab &t, const int *rr,
     for (int u = 0; u < 4; ++u) {
       const int r = rr[u];
       int E;
-      float m = ff_exp(ff_add(x[u], ff_neg(ff_from_double_int(g[u]))), E), err = 0.0f;
+      float m = ff_exp(ff_add(x[u], ff_neg(kc_ff(g[u]))), E), err = 0.0f;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         int e;
@@ -486,8 +549,8 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
                                           float mix, const FC &C, const KC &kc,
                                           double &fwd, double &rev, float &pm) {
   const int j = t.rev_idx[r];
-  // the FP64 Kc exponent first, to overlap with the FP32 forward rate
-  const double g = j >= 0 ? kc(t, r, j) : 0.0;
+  // the Kc exponent first, to overlap with the forward rate
+  const typename KcOut<KC>::type g = j >= 0 ? kc_exponent(kc, t, r, j) : typename KcOut<KC>::type{};
   float sgn;
   ff xf;
   if (PD && t.rate_kind[r] >= RATE_PLOG) {
@@ -507,7 +570,7 @@ __device__ __forceinline__ double rxn_net(const Tab &t, int r, const State &s,
   rev = 0.0;
   if (j >= 0) {
     int Er;
-    const float pr = ff_exp(ff_add(xf, ff_neg(ff_from_double_int(g))), Er);
+    const float pr = ff_exp(ff_add(xf, ff_neg(kc_ff(g))), Er);
     const float mr = sgn * product(pr, t.px_sp, t.px_nint, t.px_nu, t.px_ptr[r],
                                    t.px_ptr[r + 1], C, Er);
     rev = assemble(mr, Er);

@@ -104,13 +104,17 @@ def fp64_slots(tables, precision, exp_slots):
         ``exp_slots``, the measured FP64-pipe cost of the cheapest FP64
         exponential of this library (the table exp: FP64 FMA rate / its
         rate, ~9); logs and powers cost more, so this undercounts.
-    precision "mixed": only what the mixed split keeps in FP64 (the
-        equilibrium-constant exponent, the forward - reverse subtraction,
-        the wdot accumulation): 6 FMAs per Kc polynomial (per T_common
-        group), one subtraction per reversible reaction, one multiply per
-        reaction with a pres_mod term, one FMA per nonzero net
-        stoichiometric coefficient.
-    precision "rates": the mixed split without the accumulation (the rates
+    precision "mixed": only what the mixed one-state-per-thread kernel
+        keeps in FP64: one subtraction (forward - reverse) per reversible
+        reaction, one multiply per reaction with a pres_mod term, one FMA
+        per nonzero net stoichiometric coefficient (the wdot accumulation).
+        Its equilibrium-constant exponents run as float-float on the FP32
+        pipe when every reaction has a single T_common group; with several,
+        the kernel evaluates the FP64 polynomials, 6 FMAs per group.
+    precision "mixed_tile": the mixed split of the large-mechanism state
+        tile, which keeps the Kc exponents in FP64 (6 FMAs per T_common
+        group) beside the same subtraction, multiplies and accumulation.
+    precision "rates": mixed_tile without the accumulation (the rates
         producer of the tensor-core contraction, whose products and sums
         run on the tensor cores).
     Returns dict(slots=..., parts={...}).
@@ -125,13 +129,15 @@ def fp64_slots(tables, precision, exp_slots):
         w = work(t)
         parts = {"algebraic": w["flops"] / 2.0,
                  "transcendental": w["transcendentals"] * float(exp_slots)}
-    elif precision in ("mixed", "rates"):
-        parts = {"kc_exponent": 6.0 * groups, "net_rate": float(NREV),
-                 "pres_mod_product": float(n_pm)}
-        if precision == "mixed":
+    elif precision in ("mixed", "mixed_tile", "rates"):
+        single = all(int(t["kc_ptr"][j + 1]) - int(t["kc_ptr"][j]) <= 1 for j in range(NREV))
+        parts = {"net_rate": float(NREV), "pres_mod_product": float(n_pm)}
+        if precision != "mixed" or not single:
+            parts["kc_exponent"] = 6.0 * groups
+        if precision != "rates":
             parts["accumulation"] = float(nnz)
     else:
-        raise ValueError("precision must be fp64, mixed or rates")
+        raise ValueError("precision must be fp64, mixed, mixed_tile or rates")
     return {"slots": float(sum(parts.values())), "parts": parts}
 
 

@@ -50,7 +50,7 @@ typedef struct crs_mech crs_mech;
 /* Evaluation modes of crs_wdot. */
 #define CRS_MODE_FP64 0        /* FP64 throughout; <=1e-12 of the reference */
 #define CRS_MODE_FP64_STRICT 1 /* FP64 in the reference's operation order */
-#define CRS_MODE_MIXED 2       /* FP32 bulk, FP64 Kc exponent/net rate/sum */
+#define CRS_MODE_MIXED 2       /* FP32 bulk, float-float Kc exponent, FP64 net rate/sum */
 /* The arithmetic of CRS_MODE_FP64 / CRS_MODE_MIXED with a fixed thread
  * layout: one state per thread (TPS) or one state per warp (WARP).  The
  * default modes pick the faster layout that fits the mechanism.

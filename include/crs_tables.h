@@ -64,6 +64,11 @@ struct ImgLayout {
   // exponent polynomial with ln(prefactor) folded into c0; built when every
   // reaction has a single T_common group (kc_single = 1)
   int kc_poly, kc_single;
+  // derived f32 section (mixed kernels): the same polynomials as float-
+  // float pairs, per reversible reaction two 16-float blocks (lo, hi), each
+  // [c0..c5 as (h, l), -c6 as (h, l), T_common as a double]; built with
+  // kc_poly
+  int kc_mix;
   // derived sections (mixed, one state per thread): the net-nu species as
   // int16 and each nu as the top 16 bits of its double (nu_hi_exact = 1 when
   // every nu's other 48 bits are zero, i.e. the pair is exact)
@@ -101,7 +106,7 @@ struct Tab {
   const int16_t *rfac, *pfac;
   const int32_t *dperm, *spc_ptr, *spc_r, *lane_ptr, *lane_sp;
   const double *spc_nu;
-  const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f;
+  const float *rate_ff, *inv_mw_f, *troe_ff, *sri_ff, *eff_f, *kc_mix;
   const double *rate_x, *kc_lpref, *troe_x, *sri_x, *sp_gibbs, *exptab, *logtab, *kc_poly,
       *sp_thermo;
   int kc_single;
@@ -144,6 +149,7 @@ CRS_HD inline Tab make_tab2(const unsigned char *near,
   CRS_I(dperm); CRS_I(spc_ptr); CRS_I(spc_r); CRS_I(lane_ptr); CRS_I(lane_sp);
   CRS_F(spc_nu);
   CRS_S(rate_ff); CRS_S(inv_mw_f); CRS_S(troe_ff); CRS_S(sri_ff); CRS_S(eff_f);
+  CRS_S(kc_mix);
   CRS_F(inv_mw); CRS_F(rate_par); CRS_F(rx_nu); CRS_F(px_nu); CRS_F(kc_tmid);
   CRS_F(kc_lo); CRS_F(kc_hi); CRS_F(kc_pref); CRS_F(pm_eff_val);
   CRS_F(pm_troe); CRS_F(pm_sri); CRS_F(nu_val); CRS_F(sp_tmid); CRS_F(sp_lo);

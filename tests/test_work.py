@@ -23,22 +23,29 @@ def _bench():
 def test_slots_follow_the_tables(synth_mech):
     t = synth_mech("gri53").tables
     R, NREV = int(t["dims"][1]), int(t["dims"][2])
+    tile = work.fp64_slots(t, "mixed_tile", 9.0)
+    assert tile["parts"]["kc_exponent"] == 6 * int(t["kc_ptr"][NREV])
+    assert tile["parts"]["net_rate"] == NREV
+    assert tile["parts"]["accumulation"] == int(t["nu_ptr"][R])
+    # one T_common group per reaction: the one-state-per-thread kernel forms
+    # the Kc exponents in float-float, off the FP64 pipe
     mixed = work.fp64_slots(t, "mixed", 9.0)
-    assert mixed["parts"]["kc_exponent"] == 6 * int(t["kc_ptr"][NREV])
-    assert mixed["parts"]["net_rate"] == NREV
-    assert mixed["parts"]["accumulation"] == int(t["nu_ptr"][R])
+    assert "kc_exponent" not in mixed["parts"]
+    assert mixed["slots"] == tile["slots"] - tile["parts"]["kc_exponent"]
     rates = work.fp64_slots(t, "rates", 9.0)
-    assert rates["slots"] == mixed["slots"] - mixed["parts"]["accumulation"]
+    assert rates["slots"] == tile["slots"] - tile["parts"]["accumulation"]
     w = work.work(t)
     full = work.fp64_slots(t, "fp64", 9.0)
     assert full["slots"] == w["flops"] / 2 + 9 * w["transcendentals"]
-    # the FP64 split does strictly more FP64 work than the mixed one
-    assert full["slots"] > mixed["slots"] > rates["slots"] > 0
+    # the FP64 split does strictly more FP64 work than the mixed ones
+    assert full["slots"] > tile["slots"] > rates["slots"] > 0
+    assert tile["slots"] > mixed["slots"] > 0
     with pytest.raises(ValueError):
         work.fp64_slots(t, "fp32", 9.0)
 
 
-@pytest.mark.parametrize("precision,gemm", [("fp64", False), ("mixed", False), ("rates", True)])
+@pytest.mark.parametrize("precision,gemm", [("fp64", False), ("mixed", False), ("mixed_tile", False),
+                                            ("rates", True)])
 def test_roofline_fraction_is_one_at_the_bound(precision, gemm, synth_mech):
     b = _bench()
     t = synth_mech("gri53").tables
@@ -51,3 +58,16 @@ def test_roofline_fraction_is_one_at_the_bound(precision, gemm, synth_mech):
     slower = b._roofline(t, precision, 0.5e9 / bound_ns, peaks, N, gemm=gemm)
     assert slower["frac"] == pytest.approx(0.5, rel=1e-12)
     assert at_bound["exp_price_slots"] == pytest.approx(9.2)
+
+
+def test_mixed_counts_fp64_kc_with_several_groups(golden):
+    """A mechanism whose reactions span several T_common groups keeps the
+    FP64 Kc polynomials in the mixed one-state-per-thread kernel, and the
+    model counts them."""
+    mech, _ = golden("features")
+    t = mech.tables
+    NREV = int(t["dims"][2])
+    assert any(int(t["kc_ptr"][j + 1]) - int(t["kc_ptr"][j]) > 1 for j in range(NREV))
+    mixed = work.fp64_slots(t, "mixed", 9.0)
+    assert mixed["parts"]["kc_exponent"] == 6 * int(t["kc_ptr"][NREV])
+    assert mixed["slots"] == work.fp64_slots(t, "mixed_tile", 9.0)["slots"]
