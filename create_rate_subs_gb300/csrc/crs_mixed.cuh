@@ -238,12 +238,12 @@ __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) {
 
 // Exponent of the equilibrium constant of reversible reaction j (with ln
 // of its prefactor) as float-float, entirely on the FP32 pipe, for the
-// mixed kernels when every reaction has a single T_common group: the
-// polynomial of KcPoly1 in the same Horner order,
+// mixed one-state-per-thread kernel when every reaction has a single
+// T_common group: the polynomial of KcPoly1 in the same Horner order,
 //   c0 + c1 ln T + T (c2 + T (c3 + T (c4 + c5 T))) - c6 / T,
 // with float-float coefficients (kc_mix) and float-float T, ln T and 1/T.
-// Seven multiply-adds of ~2^-44 relative error: an absolute error near
-// 1e-11 for exponents of a few hundred, against FP32 rates that notice
+// Seven multiply-adds of ~2^-44 relative error: an absolute error of a few
+// 1e-12 for exponents of a few hundred, against FP32 rates that notice
 // 1e-7; the FP64 pipe, which retires 1/64 of the FP32 pipe's operations on
 // GB300, does none of it.
 struct KcMix {
