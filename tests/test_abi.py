@@ -98,3 +98,18 @@ def test_inspect_large_mechanism(synth_mech):
     # the 561-species tables do not fit in shared memory: the warp kernels
     # read them through L1 (the per-thread kernels are refused at launch)
     assert out[0] > 227 * 1024
+
+
+@pytest.mark.parametrize("name", ["small", "gri53"])
+def test_mixed_kc_section_is_last_and_outside_strict_staging(name, synth_mech):
+    """The mixed kernel's float-float Kc polynomials (128 B per reversible
+    reaction) are the image's last section: every other section keeps its
+    offset, and the strict kernel stages only the bytes before them
+    (crs_mech_inspect out[5] = those bytes + its per-thread columns)."""
+    mech = synth_mech(name)
+    lib = _lib.load()
+    out = (ctypes.c_int64 * 6)()
+    assert lib.crs_mech_inspect(mech.blob, len(mech.blob), out) == 0, _lib.last_error()
+    strict_staged = out[5] - 2 * mech.n_species * 128 * 8
+    assert strict_staged % 16 == 0
+    assert out[0] - strict_staged == 128 * mech.n_rev + 16  # the section + its 16 B pad
