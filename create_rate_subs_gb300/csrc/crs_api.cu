@@ -65,11 +65,17 @@ bool build_fast_tables(const std::vector<unsigned char> &img,
 namespace host {
 void eval_conc(const Tab &t, double T, double pres, const double *y, double *y_N,
                double *mw_avg, double *rho, double *conc);
-void eval_rxn_rates(const Tab &t, double T, double pres, const double *C, double *fwd,
-                    double *rev);
-void get_rxn_pres_mod(const Tab &t, double T, double pres, const double *C, double *pm);
-void eval_spec_rates(const Tab &t, const double *fwd, const double *rev, const double *pm,
-                     double *sp_rates, double *dy_N);
+// Lists of the branch-free host paths, built once per mechanism (NULL: the
+// generic path).
+struct Aux;
+Aux *make_aux(const Tab &t);
+void free_aux(Aux *a);
+void eval_rxn_rates(const Tab &t, const Aux *a, double T, double pres, const double *C,
+                    double *fwd, double *rev);
+void get_rxn_pres_mod(const Tab &t, const Aux *a, double T, double pres, const double *C,
+                      double *pm);
+void eval_spec_rates(const Tab &t, const Aux *a, const double *fwd, const double *rev,
+                     const double *pm, double *sp_rates, double *dy_N);
 void eval_thermo(const Tab &t, int which, double T, double *out);
 void eval_conc_rho(const Tab &t, double T, double rho, const double *y, double *y_N,
                    double *mw_avg, double *pres, double *conc);
@@ -95,6 +101,7 @@ struct crs_mech {
   mutable std::atomic<unsigned> sched_next{0};
   std::vector<unsigned char> h_img;
   crs::Tab htab{};  // view of h_img for the per-state host functions
+  crs::host::Aux *haux = nullptr;  // their branch-free lists
   // tensor-core contraction (CRS_MODE_GEMM): nu as a bf16 matrix
   // [N_pad][2*Kh] (each row nu_k, then nu_k again for the lo half), and a
   // workspace for one chunk of states (bf16 rows + per-state exponents),
@@ -753,6 +760,7 @@ int crs_mech_load(const void *blob, size_t nbytes, crs_mech **out) {
     return rc;
   }
   m->htab = crs::make_tab(m->h_img.data(), m->L);
+  m->haux = crs::host::make_aux(m->htab);
   cudaError_t e = cudaGetDevice(&m->device);
   if (e == cudaSuccess)
     e = cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
@@ -790,6 +798,7 @@ int crs_mech_load_host(const void *blob, size_t nbytes, crs_mech **out) {
   }
   m->device = -1;
   m->htab = crs::make_tab(m->h_img.data(), m->L);
+  m->haux = crs::host::make_aux(m->htab);
   *out = m;
   return CRS_OK;
 }
@@ -857,6 +866,7 @@ int crs_mech_free(crs_mech *m) {
   if (m->d_host) cudaFree(m->d_host);
   for (cudaStream_t st : m->hs)
     if (st) cudaStreamDestroy(st);
+  crs::host::free_aux(m->haux);
   delete m;
   return CRS_OK;
 }
@@ -1157,7 +1167,7 @@ int crs_state_eval_rxn_rates(const crs_mech *m, double T, double pres, const dou
   CRS_STATE_CHECK(m, "crs_state_eval_rxn_rates");
   if (!C || (!fwd && m->L.R > 0) || (!rev && m->L.NREV > 0))
     return fail(CRS_ERR_ARG, "crs_state_eval_rxn_rates: NULL array");
-  crs::host::eval_rxn_rates(m->htab, T, pres, C, fwd, rev);
+  crs::host::eval_rxn_rates(m->htab, m->haux, T, pres, C, fwd, rev);
   return CRS_OK;
 }
 
@@ -1166,7 +1176,7 @@ int crs_state_get_rxn_pres_mod(const crs_mech *m, double T, double pres, const d
   CRS_STATE_CHECK(m, "crs_state_get_rxn_pres_mod");
   if (!C || (!pres_mod && m->L.NPM > 0))
     return fail(CRS_ERR_ARG, "crs_state_get_rxn_pres_mod: NULL array");
-  crs::host::get_rxn_pres_mod(m->htab, T, pres, C, pres_mod);
+  crs::host::get_rxn_pres_mod(m->htab, m->haux, T, pres, C, pres_mod);
   return CRS_OK;
 }
 
@@ -1176,7 +1186,7 @@ int crs_state_eval_spec_rates(const crs_mech *m, const double *fwd, const double
   if ((!fwd && m->L.R > 0) || (!rev && m->L.NREV > 0) || (!pres_mod && m->L.NPM > 0) ||
       (!sp_rates && m->L.N > 1) || !dy_N)
     return fail(CRS_ERR_ARG, "crs_state_eval_spec_rates: NULL array");
-  crs::host::eval_spec_rates(m->htab, fwd, rev, pres_mod, sp_rates, dy_N);
+  crs::host::eval_spec_rates(m->htab, m->haux, fwd, rev, pres_mod, sp_rates, dy_N);
   return CRS_OK;
 }
 
@@ -1255,21 +1265,21 @@ void eval_conc(const double T, const double pres, const double *y, double *y_N,
 void eval_rxn_rates(const double T, const double pres, const double *C,
                     double *fwd_rxn_rates, double *rev_rxn_rates) {
   if (const crs_mech *m = bound("eval_rxn_rates"))
-    crs::host::eval_rxn_rates(m->htab, T, pres, C, fwd_rxn_rates, rev_rxn_rates);
+    crs::host::eval_rxn_rates(m->htab, m->haux, T, pres, C, fwd_rxn_rates, rev_rxn_rates);
 }
 
 // rate_subs.py:761-763 (rates.h)
 void get_rxn_pres_mod(const double T, const double pres, const double *C,
                       double *pres_mod) {
   if (const crs_mech *m = bound("get_rxn_pres_mod"))
-    crs::host::get_rxn_pres_mod(m->htab, T, pres, C, pres_mod);
+    crs::host::get_rxn_pres_mod(m->htab, m->haux, T, pres, C, pres_mod);
 }
 
 // rate_subs.py:1124-1127 (rates.h)
 void eval_spec_rates(const double *fwd_rates, const double *rev_rates,
                      const double *pres_mod, double *sp_rates, double *dy_N) {
   if (const crs_mech *m = bound("eval_spec_rates"))
-    crs::host::eval_spec_rates(m->htab, fwd_rates, rev_rates, pres_mod, sp_rates, dy_N);
+    crs::host::eval_spec_rates(m->htab, m->haux, fwd_rates, rev_rates, pres_mod, sp_rates, dy_N);
 }
 
 // rate_subs.py:1497-1776 (chem_utils.h :1276-1279)
