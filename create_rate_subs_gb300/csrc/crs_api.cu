@@ -79,7 +79,8 @@ void eval_spec_rates(const Tab &t, const Aux *a, const double *fwd, const double
 void eval_thermo(const Tab &t, int which, double T, double *out);
 void eval_conc_rho(const Tab &t, double T, double rho, const double *y, double *y_N,
                    double *mw_avg, double *pres, double *conc);
-void dydt(const Tab &t, int conv, double p_or_rho, const double *y, double *dy);
+void dydt(const Tab &t, const Aux *a, int conv, double p_or_rho, const double *y,
+          double *dy);
 }  // namespace host
 }  // namespace crs
 
@@ -1211,7 +1212,7 @@ int crs_state_dydt(const crs_mech *m, int conv, double p_or_rho, const double *y
   CRS_STATE_CHECK(m, "crs_state_dydt");
   if (conv != 0 && conv != 1) return fail(CRS_ERR_ARG, "conv must be 0 or 1");
   if (!y || !dy) return fail(CRS_ERR_ARG, "crs_state_dydt: NULL array");
-  crs::host::dydt(m->htab, conv, p_or_rho, y, dy);
+  crs::host::dydt(m->htab, m->haux, conv, p_or_rho, y, dy);
   return CRS_OK;
 }
 
@@ -1315,7 +1316,7 @@ int crs_dydt_form(int conv) {
 void dydt(const double t, const double pres, const double *y, double *dy) {
   (void)t;
   if (const crs_mech *m = bound("dydt"))
-    crs::host::dydt(m->htab, g_dydt_conv.load(), pres, y, dy);
+    crs::host::dydt(m->htab, m->haux, g_dydt_conv.load(), pres, y, dy);
 }
 
 }  // extern "C"

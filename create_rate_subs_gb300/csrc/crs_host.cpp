@@ -212,13 +212,51 @@ void eval_conc_rho(const Tab &t, double T, double rho, const double *y, double *
   ref::state_eval_conc_rho(t, T, rho, y, y_N, mw_avg, pres, conc);
 }
 
-// Scratch of the calling thread (concentrations, rates, thermo columns),
-// grown on its first call for the largest mechanism it has seen.
-void dydt(const Tab &t, int conv, double p_or_rho, const double *y, double *dy) {
+// dydt (rate_subs.py:1829-2067): ref::state_dydt's sequence with the
+// three rate functions above in place of the generic ones.  Scratch of the
+// calling thread (concentrations, rates, thermo columns), grown on its
+// first call for the largest mechanism it has seen.
+void dydt(const Tab &t, const Aux *a, int conv, double p_or_rho, const double *y,
+          double *dy) {
   thread_local std::vector<double> scratch;
-  const size_t need = (size_t)ref::dydt_scratch(t);
-  if (scratch.size() < need) scratch.resize(need);
-  ref::state_dydt(t, conv, p_or_rho, y, dy, scratch.data());
+  double *s = crs::host::scratch(scratch, (size_t)ref::dydt_scratch(t));
+  if (!a) {
+    ref::state_dydt(t, conv, p_or_rho, y, dy, s);
+    return;
+  }
+  const int N = t.N;
+  double *C = s, *fwd = C + N, *rev = fwd + t.R;
+  double *pm = rev + (t.NREV > 0 ? t.NREV : 1);
+  double *c = pm + (t.NPM > 0 ? t.NPM : 1), *e = c + N;
+  const double T = y[0];
+  double y_N, mw_avg, rho, pres;
+  if (conv) {
+    rho = p_or_rho;
+    ref::state_eval_conc_rho(t, T, rho, y + 1, &y_N, &mw_avg, &pres, C);
+  } else {
+    pres = p_or_rho;
+    ref::state_eval_conc(t, T, pres, y + 1, &y_N, &mw_avg, &rho, C);
+  }
+  eval_rxn_rates(t, a, T, pres, C, fwd, rev);
+  get_rxn_pres_mod(t, a, T, pres, C, pm);
+  double dy_N;
+  eval_spec_rates(t, a, fwd, rev, pm, dy + 1, &dy_N);
+  ref::state_eval_thermo(t, conv ? 2 : 3, T, c);
+  double avg = 0.0;
+  for (int k = 0; k < N - 1; ++k) {
+    const double v = c[k] * y[k + 1];
+    avg = (k == 0) ? v : avg + v;
+  }
+  avg = (N > 1) ? avg + c[N - 1] * y_N : c[N - 1] * y_N;
+  ref::state_eval_thermo(t, conv ? 1 : 0, T, e);
+  double sum = 0.0;
+  for (int k = 0; k < N - 1; ++k) {
+    const double v = dy[k + 1] * e[k] * t.sp_mw[k];
+    sum = (k == 0) ? v : sum + v;
+  }
+  sum = (N > 1) ? sum + dy_N * e[N - 1] * t.sp_mw[N - 1] : dy_N * e[N - 1] * t.sp_mw[N - 1];
+  dy[0] = (-1.0 / (rho * avg)) * sum;
+  for (int k = 0; k < N - 1; ++k) dy[k + 1] *= (t.sp_mw[k] / rho);
 }
 
 }  // namespace host
