@@ -261,3 +261,43 @@ def test_host_only_handle_refused_by_batched_calls(golden):
     rc = hm.lib.crs_wdot(hm.h, 4, None, None, None, 4, None, 0, None)
     assert rc == 1 and "no device tables" in _lib.last_error()
     hm.close()
+
+
+@pytest.mark.parametrize("name,n", [("gri53", 300), ("large561", 24)])
+def test_host_functions_bitexact_vs_reference_build(name, n, synth_mech):
+    """The per-state host functions (their padded-factor, signed-sum and
+    grouped pres_mod paths) on fresh seeded states of the workload
+    mechanisms, against the reference's own emitted C for the same states,
+    every stage bit for bit."""
+    from oracle.oracle import RefLib
+    from create_rate_subs_gb300 import synth
+    if not RefLib.available(name):
+        pytest.skip("reference C not built here (python oracle/build_ref.py all %s)" % name)
+    mech = synth_mech(name)
+    N, R, NREV, NPM = mech.n_species, mech.n_reactions, mech.n_rev, mech.n_pdep
+    T, P, Y = synth.make_states(N, n, seed=2024)
+    want = RefLib(name).eval(T, P, Y)
+    hm = HostMech(mech)
+    lib = hm.lib
+    try:
+        for i in range(n):
+            y = np.ascontiguousarray(Y[: N - 1, i])
+            conc = np.zeros(N)
+            yN, mw, rho = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+            fwd, rev, pm = np.zeros(R), np.zeros(max(NREV, 1)), np.zeros(max(NPM, 1))
+            sp, dyN = np.zeros(N - 1), ctypes.c_double()
+            h, Ti, Pi = hm.h, float(T[i]), float(P[i])
+            _lib.check(lib.crs_state_eval_conc(h, Ti, Pi, dp(y), ctypes.byref(yN),
+                                               ctypes.byref(mw), ctypes.byref(rho), dp(conc)))
+            _lib.check(lib.crs_state_eval_rxn_rates(h, Ti, Pi, dp(conc), dp(fwd), dp(rev)))
+            _lib.check(lib.crs_state_get_rxn_pres_mod(h, Ti, Pi, dp(conc), dp(pm)))
+            _lib.check(lib.crs_state_eval_spec_rates(h, dp(fwd), dp(rev), dp(pm), dp(sp),
+                                                     ctypes.byref(dyN)))
+            assert np.array_equal(conc, want["conc"][:, i]), (name, i, "conc")
+            assert np.array_equal(fwd, want["fwd"][:, i]), (name, i, "fwd")
+            assert np.array_equal(rev[:NREV], want["rev"][:, i]), (name, i, "rev")
+            assert np.array_equal(pm[:NPM], want["pm"][:, i]), (name, i, "pm")
+            wdot = np.concatenate([sp, [dyN.value]])
+            assert np.array_equal(wdot, want["wdot"][:, i]), (name, i, "wdot")
+    finally:
+        hm.close()
