@@ -110,3 +110,93 @@ def test_cuda_target_compiles_into_a_user_kernel(tmp_path):
                                                     "-o", str(tmp_path / "user.o")],
                          capture_output=True, text=True)
     assert res.returncode == 0, res.stdout + res.stderr
+
+
+def test_c_target_drop_in_from_a_c_program(tmp_path, golden):
+    """The c target's headers with libcrs behind them, used the way an
+    integrator uses the reference's emitted C: a C program (gcc, OpenMP)
+    includes out/header.h, rates.h and chem_utils.h, binds the mechanism
+    loaded from out/mech.crs and calls the four per-state functions by the
+    reference's names from several threads; every output equals the
+    reference's golden vectors bit for bit."""
+    import shutil
+    import subprocess
+    import numpy as np
+    from conftest import REPO
+    from create_rate_subs_gb300 import build as crs_build
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    mech, g = golden("features")
+    assert _run(tmp_path, "-l", "c", "-i", MECH, "-t", THERM) == 0
+    out = tmp_path / "out"
+    N, R, NREV, NPM = (int(x) for x in g["dims"][:4])
+    n = g["T"].shape[0]
+    np.ascontiguousarray(g["T"]).tofile(str(tmp_path / "T.bin"))
+    np.ascontiguousarray(g["P"]).tofile(str(tmp_path / "P.bin"))
+    np.ascontiguousarray(g["Y"][: N - 1].T).tofile(str(tmp_path / "Y.bin"))  # per state
+    src = tmp_path / "drop_in.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "crs.h"
+#include "header.h"
+#include "rates.h"
+#include "chem_utils.h"
+
+static void *slurp(const char *f, size_t *sz) {
+  FILE *fp = fopen(f, "rb");
+  if (!fp) exit(2);
+  fseek(fp, 0, SEEK_END);
+  *sz = (size_t)ftell(fp);
+  fseek(fp, 0, SEEK_SET);
+  void *b = malloc(*sz);
+  if (fread(b, 1, *sz, fp) != *sz) exit(2);
+  fclose(fp);
+  return b;
+}
+
+int main(void) {
+  size_t sb, st, sp_, sy;
+  void *blob = slurp("out/mech.crs", &sb);
+  double *T = slurp("T.bin", &st), *P = slurp("P.bin", &sp_), *Y = slurp("Y.bin", &sy);
+  const int n = (int)(st / sizeof(double));
+  crs_mech *m = NULL;
+  if (crs_mech_load_host(blob, sb, &m) != CRS_OK) return 3;
+  if (crs_bind(m) != CRS_OK) return 3;
+  double *o = malloc(sizeof(double) * (size_t)n * (NSP + NRXN + NRXN_REV + NPDEP + NSP));
+  const size_t w = NSP + NRXN + NRXN_REV + NPDEP + NSP;
+#pragma omp parallel for schedule(static, 1)
+  for (int i = 0; i < n; ++i) {
+    double *conc = o + (size_t)i * w, *fwd = conc + NSP, *rev = fwd + NRXN;
+    double *pm = rev + NRXN_REV, *sp = pm + NPDEP;
+    double y_N, mw, rho;
+    eval_conc(T[i], P[i], Y + (size_t)i * (NSP - 1), &y_N, &mw, &rho, conc);
+    eval_rxn_rates(T[i], P[i], conc, fwd, rev);
+    get_rxn_pres_mod(T[i], P[i], conc, pm);
+    eval_spec_rates(fwd, rev, pm, sp, &sp[NSP - 1]);
+  }
+  FILE *fo = fopen("out.bin", "wb");
+  fwrite(o, sizeof(double), (size_t)n * w, fo);
+  fclose(fo);
+  crs_bind(NULL);
+  crs_mech_free(m);
+  return 0;
+}
+""")
+    libdir = os.path.dirname(crs_build.build())
+    exe = tmp_path / "drop_in"
+    cc = subprocess.run([gcc, "-O2", "-fopenmp", "-I", str(out), "-I", os.path.join(REPO, "include"),
+                         str(src), "-L", libdir, "-lcrs", "-Wl,-rpath," + libdir, "-o", str(exe)],
+                        capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr[-2000:]
+    env = dict(os.environ, OMP_NUM_THREADS="4")
+    run = subprocess.run([str(exe)], cwd=str(tmp_path), env=env, capture_output=True, text=True)
+    assert run.returncode == 0, (run.returncode, run.stderr[-2000:])
+    w = N + R + NREV + NPM + N
+    o = np.fromfile(str(tmp_path / "out.bin")).reshape(n, w).T
+    assert np.array_equal(o[:N], g["conc"])
+    assert np.array_equal(o[N:N + R], g["fwd"])
+    assert np.array_equal(o[N + R:N + R + NREV], g["rev"])
+    assert np.array_equal(o[N + R + NREV:N + R + NREV + NPM], g["pm"])
+    assert np.array_equal(o[N + R + NREV + NPM:], g["wdot"])
